@@ -1,0 +1,517 @@
+// ppi_gpu_api.cu -- host implementation of the C ABI in include/ppi_gpu.h.
+//
+// State that the reference keeps in one process-global struct
+// (src/interpreter/accelerator.cc:56) lives in a handle here.  One generation
+// is: three H2D copies (phenotype, ephemeral, size, as accelerator.cc:668-684),
+// the translator kernel, the evaluator kernel (fitness, alpha*size and arg-min
+// fused), and one D2H copy of fitness + best index into pinned staging.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "ppi_internal.cuh"
+#include "ppi_decode.cuh"
+
+using namespace ppi;
+
+struct ppi_gpu {
+   ppi_gpu_config cfg{};
+   std::vector<float> cost;
+   std::string err;
+   int device = 0, sm_count = 0;
+   cudaStream_t stream = nullptr;
+   cudaEvent_t ev0 = nullptr, ev1 = nullptr, evm = nullptr;
+   // symbol lookup
+   int2* d_lut = nullptr;
+   int lut_min = 0, lut_len = 0;
+   float* d_cost = nullptr;
+   // dataset
+   float* d_data = nullptr;
+   int nlin = 0, ncol = 0, ld = 0;
+   bool have_data = false;
+   int lanes = 1, block = 128, grid = 1;
+   size_t smem = 0;
+   // per-generation buffers (capacity population_size)
+   int32_t* d_ph = nullptr;
+   float* d_eph = nullptr;
+   int32_t* d_size = nullptr;
+   uint2* d_code = nullptr;
+   int code_stride = 0;
+   int2* d_meta = nullptr;
+   uint2* d_work = nullptr;
+   float* d_fit = nullptr;
+   unsigned long long* d_key = nullptr;
+   unsigned* d_counters = nullptr;
+   int32_t* d_best = nullptr;
+   int* d_status = nullptr;
+   float* d_pred = nullptr;
+   // pinned staging of the outputs
+   float* h_fit = nullptr;
+   int32_t* h_best = nullptr;
+   int* h_status = nullptr;
+   // pending split call
+   bool pending = false;
+   int pending_n = 0;
+   float* out_fit = nullptr;
+   int32_t* out_best = nullptr;
+   // device decode
+   DecodeTables dec{};
+   uint8_t* d_genomes = nullptr;
+   size_t genome_cap = 0;
+   uint32_t* d_frames = nullptr;
+   size_t frames_cap = 0;
+   float last_ms = 0.0f;
+   int last_launches = 0;
+};
+
+namespace {
+
+ppi_status fail(ppi_gpu* h, ppi_status s, const std::string& msg) {
+   if (h) h->err = msg;
+   return s;
+}
+
+#define PPI_CUDA(h, call)                                                                   \
+   do {                                                                                     \
+      cudaError_t e_ = (call);                                                              \
+      if (e_ != cudaSuccess)                                                                \
+         return fail((h), e_ == cudaErrorMemoryAllocation ? PPI_ERR_OUT_OF_MEMORY : PPI_ERR_CUDA, \
+                     std::string(#call) + ": " + cudaGetErrorString(e_));                   \
+   } while (0)
+
+template <class T>
+cudaError_t dalloc(T** p, size_t count) {
+   *p = nullptr;
+   if (count == 0) count = 1;
+   return cudaMalloc(reinterpret_cast<void**>(p), count * sizeof(T));
+}
+
+void free_all(ppi_gpu* h) {
+   cudaFree(h->d_lut); cudaFree(h->d_cost); cudaFree(h->d_data);
+   cudaFree(h->d_ph); cudaFree(h->d_eph); cudaFree(h->d_size); cudaFree(h->d_code);
+   cudaFree(h->d_meta); cudaFree(h->d_work); cudaFree(h->d_fit); cudaFree(h->d_key);
+   cudaFree(h->d_counters); cudaFree(h->d_best); cudaFree(h->d_status); cudaFree(h->d_pred);
+   cudaFree(h->d_genomes); cudaFree(h->d_frames);
+   free_decode_tables(&h->dec);
+   cudaFreeHost(h->h_fit); cudaFreeHost(h->h_best); cudaFreeHost(h->h_status);
+   if (h->ev0) cudaEventDestroy(h->ev0);
+   if (h->ev1) cudaEventDestroy(h->ev1);
+   if (h->evm) cudaEventDestroy(h->evm);
+   if (h->stream) cudaStreamDestroy(h->stream);
+}
+
+// Evaluator geometry for the current dataset and lane count.
+ppi_status plan(ppi_gpu* h) {
+   const int L = h->lanes;
+   int P;
+   if (h->cfg.strategy == PPI_STRATEGY_PDP && L % (32 * kR) == 0 && L / kR <= 128) {
+      P = L / kR;   // lane == tile position: register accumulation
+   } else {
+      const int need = (h->cfg.strategy == PPI_STRATEGY_DP) ? L : std::min(h->nlin, 128 * kR);
+      P = std::min(128, std::max(32, ((need + kR - 1) / kR + 31) / 32 * 32));
+   }
+   if (h->cfg.strategy == PPI_STRATEGY_DP && L > P * kR)
+      return fail(h, PPI_ERR_UNSUPPORTED, "DP lanes above 1024 records per group are not supported");
+   size_t smem = evaluate_smem_bytes(h->code_stride, h->ncol, P, L);
+   while (smem > 200 * 1024 && P > 32 && !(h->cfg.strategy == PPI_STRATEGY_DP && L > (P / 2) * kR)) {
+      P /= 2;
+      smem = evaluate_smem_bytes(h->code_stride, h->ncol, P, L);
+   }
+   if (smem > 200 * 1024)
+      return fail(h, PPI_ERR_UNSUPPORTED, "dataset has too many columns for one shared-memory tile");
+   int per_sm = 0;
+   PPI_CUDA(h, evaluate_occupancy(h->cfg.math, P, smem, &per_sm));
+   if (per_sm < 1) return fail(h, PPI_ERR_UNSUPPORTED, "evaluator does not fit on an SM");
+   h->block = P;
+   h->smem = smem;
+   h->grid = std::max(1, std::min(h->cfg.population_size, per_sm * h->sm_count));
+   return PPI_OK;
+}
+
+ppi_status check_ready(ppi_gpu* h, int n) {
+   if (!h) return PPI_ERR_INVALID_ARGUMENT;
+   if (!h->have_data) return fail(h, PPI_ERR_NOT_READY, "no dataset: call ppi_gpu_set_dataset first");
+   if (h->pending) return fail(h, PPI_ERR_NOT_READY, "an evaluate_launch is still pending");
+   if (n < 1 || n > h->cfg.population_size)
+      return fail(h, PPI_ERR_INVALID_ARGUMENT, "n must be in [1, population_size]");
+   return PPI_OK;
+}
+
+ppi_status enqueue(ppi_gpu* h, const int32_t* d_ph, const float* d_eph, const int32_t* d_size,
+                   int n, float alpha, float* d_fit, int32_t* d_best, cudaStream_t s) {
+   TranslateArgs t{};
+   t.phenotype = d_ph; t.ephemeral = d_eph; t.size = d_size; t.n = n;
+   t.max_size = h->cfg.max_size; t.ncol = h->ncol;
+   t.lut = h->d_lut; t.lut_min = h->lut_min; t.lut_len = h->lut_len;
+   t.code = h->d_code; t.code_stride = h->code_stride; t.meta = h->d_meta; t.work = h->d_work;
+   t.best_key = h->d_key; t.counters = h->d_counters; t.status = h->d_status;
+   EvalArgs e{};
+   e.data = h->d_data; e.nlin = h->nlin; e.ncol = h->ncol; e.ld = h->ld;
+   e.code = h->d_code; e.code_stride = h->code_stride; e.meta = h->d_meta; e.size = d_size;
+   e.n = n; e.alpha = alpha; e.ef = h->cfg.error_fn; e.reduce_max = h->cfg.reduce_max ? 1 : 0;
+   e.prot = h->cfg.protected_fns ? 1 : 0; e.cost = h->d_cost; e.cost_n = h->cfg.cost_n;
+   e.strategy = h->cfg.strategy; e.lanes = h->lanes; e.fitness = d_fit; e.best_key = h->d_key;
+   e.counters = h->d_counters; e.best_index = d_best; e.status = h->d_status;
+   PPI_CUDA(h, cudaEventRecord(h->ev0, s));
+   PPI_CUDA(h, launch_translate(t, s));
+   PPI_CUDA(h, cudaEventRecord(h->evm, s));
+   PPI_CUDA(h, launch_evaluate(h->cfg.math, e, h->block, std::min(h->grid, n), h->smem, s));
+   PPI_CUDA(h, cudaEventRecord(h->ev1, s));
+   h->last_launches = 2;
+   return PPI_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* ppi_gpu_version(void) { return "ppi_gpu 1 sm_103a"; }
+
+const char* ppi_gpu_last_error(const ppi_gpu* h) { return h ? h->err.c_str() : "null handle"; }
+
+ppi_status ppi_gpu_create(const ppi_gpu_config* c, ppi_gpu** out) {
+   if (!c || !out) return PPI_ERR_INVALID_ARGUMENT;
+   *out = nullptr;
+   if (c->max_size < 1 || c->max_size > 65535 || c->population_size < 1 ||
+       c->strategy < 0 || c->strategy > 2 || c->error_fn < 0 || c->error_fn > 3 || c->math < 0 ||
+       c->math > 2 || c->lanes > kMaxLanes || c->n_symbols < 0 ||
+       (c->n_symbols > 0 && !c->symbols))
+      return PPI_ERR_INVALID_ARGUMENT;
+   if (c->error_fn == PPI_EF_COST && (!c->cost || c->cost_n < 1 || c->cost_n > 4096))
+      return PPI_ERR_INVALID_ARGUMENT;
+   ppi_gpu* h = new ppi_gpu();
+   h->cfg = *c;
+   h->cfg.symbols = nullptr;
+   h->cfg.cost = nullptr;
+   h->device = c->device;
+   auto bail = [&](ppi_status s) { free_all(h); delete h; return s; };
+   int ndev = 0;
+   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return bail(PPI_ERR_CUDA);
+   if (c->device < 0 || c->device >= ndev) return bail(PPI_ERR_INVALID_ARGUMENT);
+   if (cudaSetDevice(c->device) != cudaSuccess) return bail(PPI_ERR_CUDA);
+   cudaDeviceGetAttribute(&h->sm_count, cudaDevAttrMultiProcessorCount, c->device);
+   if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess ||
+       cudaEventCreate(&h->ev0) != cudaSuccess || cudaEventCreate(&h->ev1) != cudaSuccess || cudaEventCreate(&h->evm) != cudaSuccess)
+      return bail(PPI_ERR_CUDA);
+   // Symbol -> op table, dense over [min symbol, max symbol].
+   int mn = 0, mx = -1;
+   for (int i = 0; i < c->n_symbols; ++i) {
+      if (c->symbols[i].op < 0 || c->symbols[i].op >= PPI_OP_COUNT) return bail(PPI_ERR_INVALID_ARGUMENT);
+      if (i == 0 || c->symbols[i].symbol < mn) mn = c->symbols[i].symbol;
+      if (i == 0 || c->symbols[i].symbol > mx) mx = c->symbols[i].symbol;
+   }
+   if (c->n_symbols > 0 && (long long)mx - mn + 1 > (1 << 22)) return bail(PPI_ERR_UNSUPPORTED);
+   std::vector<int2> lut(c->n_symbols > 0 ? (size_t)(mx - mn + 1) : 1,
+                         make_int2(PPI_OP_INVALID, 0x7fc00000));
+   for (int i = 0; i < c->n_symbols; ++i) {
+      int32_t bits;
+      std::memcpy(&bits, &c->symbols[i].value, 4);
+      lut[(size_t)(c->symbols[i].symbol - mn)] = make_int2(c->symbols[i].op, bits);
+   }
+   h->lut_min = mn;
+   h->lut_len = c->n_symbols > 0 ? mx - mn + 1 : 0;
+   const size_t pop = (size_t)c->population_size, ms = (size_t)c->max_size;
+   h->code_stride = 2 * c->max_size + 2;
+   if (dalloc(&h->d_lut, lut.size()) != cudaSuccess ||
+       dalloc(&h->d_ph, pop * ms) != cudaSuccess || dalloc(&h->d_eph, pop * ms) != cudaSuccess ||
+       dalloc(&h->d_size, pop) != cudaSuccess ||
+       dalloc(&h->d_code, pop * (size_t)h->code_stride) != cudaSuccess ||
+       dalloc(&h->d_meta, pop) != cudaSuccess || dalloc(&h->d_work, pop * 2 * ms) != cudaSuccess ||
+       dalloc(&h->d_fit, pop) != cudaSuccess || dalloc(&h->d_key, 1) != cudaSuccess ||
+       dalloc(&h->d_counters, 2) != cudaSuccess || dalloc(&h->d_best, 1) != cudaSuccess ||
+       dalloc(&h->d_status, 1) != cudaSuccess ||
+       cudaMallocHost(reinterpret_cast<void**>(&h->h_fit), pop * sizeof(float)) != cudaSuccess ||
+       cudaMallocHost(reinterpret_cast<void**>(&h->h_best), sizeof(int32_t)) != cudaSuccess ||
+       cudaMallocHost(reinterpret_cast<void**>(&h->h_status), sizeof(int)) != cudaSuccess)
+      return bail(PPI_ERR_OUT_OF_MEMORY);
+   if (cudaMemcpy(h->d_lut, lut.data(), lut.size() * sizeof(int2), cudaMemcpyHostToDevice) != cudaSuccess)
+      return bail(PPI_ERR_CUDA);
+   if (c->error_fn == PPI_EF_COST) {
+      h->cost.assign(c->cost, c->cost + (size_t)c->cost_n * c->cost_n);
+      if (dalloc(&h->d_cost, h->cost.size()) != cudaSuccess ||
+          cudaMemcpy(h->d_cost, h->cost.data(), h->cost.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess)
+         return bail(PPI_ERR_OUT_OF_MEMORY);
+   }
+   *out = h;
+   return PPI_OK;
+}
+
+ppi_status ppi_gpu_destroy(ppi_gpu* h) {
+   if (!h) return PPI_ERR_INVALID_ARGUMENT;
+   cudaSetDevice(h->device);
+   if (h->stream) cudaStreamSynchronize(h->stream);
+   free_all(h);
+   delete h;
+   return PPI_OK;
+}
+
+ppi_status ppi_gpu_set_dataset_rowmajor(ppi_gpu* h, const float* data, int32_t nlin, int32_t ncol) {
+   if (!h || !data || nlin < 1 || ncol < 1) return fail(h, PPI_ERR_INVALID_ARGUMENT, "bad dataset");
+   std::vector<const float*> rows((size_t)nlin);
+   for (int i = 0; i < nlin; ++i) rows[i] = data + (size_t)i * ncol;
+   return ppi_gpu_set_dataset(h, rows.data(), nlin, ncol);
+}
+
+ppi_status ppi_gpu_set_dataset(ppi_gpu* h, const float* const* rows, int32_t nlin, int32_t ncol) {
+   if (!h) return PPI_ERR_INVALID_ARGUMENT;
+   if (!rows || nlin < 1 || ncol < 1) return fail(h, PPI_ERR_INVALID_ARGUMENT, "bad dataset");
+   if (h->pending) return fail(h, PPI_ERR_NOT_READY, "an evaluate_launch is still pending");
+   PPI_CUDA(h, cudaSetDevice(h->device));
+   const int ld = (nlin + kColumnPad - 1) / kColumnPad * kColumnPad;
+   // Column-major copy (the reference's -transpose layout, accelerator.cc:413-419),
+   // zero-padded to a multiple of kColumnPad records.
+   std::vector<float> cm((size_t)ld * ncol, 0.0f);
+   for (int i = 0; i < nlin; ++i) {
+      if (!rows[i]) return fail(h, PPI_ERR_INVALID_ARGUMENT, "null dataset row");
+      for (int j = 0; j < ncol; ++j) cm[(size_t)j * ld + i] = rows[i][j];
+   }
+   cudaFree(h->d_data);
+   h->d_data = nullptr;
+   h->have_data = false;
+   PPI_CUDA(h, dalloc(&h->d_data, cm.size()));
+   PPI_CUDA(h, cudaMemcpy(h->d_data, cm.data(), cm.size() * sizeof(float), cudaMemcpyHostToDevice));
+   cudaFree(h->d_pred);
+   h->d_pred = nullptr;
+   PPI_CUDA(h, dalloc(&h->d_pred, (size_t)nlin));
+   h->nlin = nlin;
+   h->ncol = ncol;
+   h->ld = ld;
+   // Lane count: -cl-mls when given; else the reference's rule on a device
+   // with 1024-wide work-groups and 152 compute units (accelerator.cc:296-330).
+   int L = h->cfg.lanes;
+   if (h->cfg.strategy == PPI_STRATEGY_PP) L = 1;
+   else if (L <= 0 && h->cfg.strategy == PPI_STRATEGY_PDP) L = std::min(nlin, 1024);
+   else if (L <= 0) L = std::min(1024, (int)std::ceil(nlin / (float)std::max(1, h->sm_count)));
+   else if (h->cfg.strategy == PPI_STRATEGY_PDP) L = std::min(L, nlin);
+   if (L < 1 || L > kMaxLanes) return fail(h, PPI_ERR_UNSUPPORTED, "lane count out of range");
+   h->lanes = L;
+   ppi_status s = plan(h);
+   if (s != PPI_OK) return s;
+   h->have_data = true;
+   return PPI_OK;
+}
+
+ppi_status ppi_gpu_evaluate_launch(ppi_gpu* h, const int32_t* ph, const float* eph,
+                                   const int32_t* size, int32_t n, float alpha, float* fitness,
+                                   int32_t* best_index) {
+   ppi_status s = check_ready(h, n);
+   if (s != PPI_OK) return s;
+   if (!ph || !eph || !size || !fitness) return fail(h, PPI_ERR_INVALID_ARGUMENT, "null argument");
+   PPI_CUDA(h, cudaSetDevice(h->device));
+   const size_t ms = (size_t)h->cfg.max_size;
+   PPI_CUDA(h, cudaMemcpyAsync(h->d_ph, ph, (size_t)n * ms * 4, cudaMemcpyHostToDevice, h->stream));
+   PPI_CUDA(h, cudaMemcpyAsync(h->d_eph, eph, (size_t)n * ms * 4, cudaMemcpyHostToDevice, h->stream));
+   PPI_CUDA(h, cudaMemcpyAsync(h->d_size, size, (size_t)n * 4, cudaMemcpyHostToDevice, h->stream));
+   s = enqueue(h, h->d_ph, h->d_eph, h->d_size, n, alpha, h->d_fit, h->d_best, h->stream);
+   if (s != PPI_OK) return s;
+   PPI_CUDA(h, cudaMemcpyAsync(h->h_fit, h->d_fit, (size_t)n * 4, cudaMemcpyDeviceToHost, h->stream));
+   PPI_CUDA(h, cudaMemcpyAsync(h->h_best, h->d_best, 4, cudaMemcpyDeviceToHost, h->stream));
+   PPI_CUDA(h, cudaMemcpyAsync(h->h_status, h->d_status, 4, cudaMemcpyDeviceToHost, h->stream));
+   h->pending = true;
+   h->pending_n = n;
+   h->out_fit = fitness;
+   h->out_best = best_index;
+   return PPI_OK;
+}
+
+ppi_status ppi_gpu_evaluate_wait(ppi_gpu* h) {
+   if (!h) return PPI_ERR_INVALID_ARGUMENT;
+   if (!h->pending) return fail(h, PPI_ERR_NOT_READY, "no pending evaluate_launch");
+   h->pending = false;
+   PPI_CUDA(h, cudaStreamSynchronize(h->stream));
+   std::memcpy(h->out_fit, h->h_fit, (size_t)h->pending_n * sizeof(float));
+   if (h->out_best) *h->out_best = *h->h_best;
+   cudaEventElapsedTime(&h->last_ms, h->ev0, h->ev1);
+   if (*h->h_status & kStatusUnsupportedProgram)
+      return fail(h, PPI_ERR_UNSUPPORTED,
+                  "a malformed program needs a deeper stack than the generic interpreter's");
+   return PPI_OK;
+}
+
+ppi_status ppi_gpu_evaluate(ppi_gpu* h, const int32_t* ph, const float* eph, const int32_t* size,
+                            int32_t n, float alpha, float* fitness, int32_t* best_index) {
+   ppi_status s = ppi_gpu_evaluate_launch(h, ph, eph, size, n, alpha, fitness, best_index);
+   if (s != PPI_OK) return s;
+   return ppi_gpu_evaluate_wait(h);
+}
+
+ppi_status ppi_gpu_evaluate_device(ppi_gpu* h, const int32_t* d_ph, const float* d_eph,
+                                   const int32_t* d_size, int32_t n, float alpha, float* d_fit,
+                                   int32_t* d_best, void* stream) {
+   ppi_status s = check_ready(h, n);
+   if (s != PPI_OK) return s;
+   if (!d_ph || !d_eph || !d_size || !d_fit || !d_best)
+      return fail(h, PPI_ERR_INVALID_ARGUMENT, "null argument");
+   PPI_CUDA(h, cudaSetDevice(h->device));
+   return enqueue(h, d_ph, d_eph, d_size, n, alpha, d_fit, d_best,
+                  reinterpret_cast<cudaStream_t>(stream));
+}
+
+ppi_status ppi_gpu_predict(ppi_gpu* h, const int32_t* ph, const float* eph, int32_t size,
+                           float* out) {
+   ppi_status s = check_ready(h, 1);
+   if (s != PPI_OK) return s;
+   if (!ph || !eph || !out || size < 0 || size > h->cfg.max_size)
+      return fail(h, PPI_ERR_INVALID_ARGUMENT, "bad program");
+   PPI_CUDA(h, cudaSetDevice(h->device));
+   if (size > 0) {
+      PPI_CUDA(h, cudaMemcpyAsync(h->d_ph, ph, (size_t)size * 4, cudaMemcpyHostToDevice, h->stream));
+      PPI_CUDA(h, cudaMemcpyAsync(h->d_eph, eph, (size_t)size * 4, cudaMemcpyHostToDevice, h->stream));
+   }
+   PPI_CUDA(h, cudaMemcpyAsync(h->d_size, &size, 4, cudaMemcpyHostToDevice, h->stream));
+   TranslateArgs t{};
+   t.phenotype = h->d_ph; t.ephemeral = h->d_eph; t.size = h->d_size; t.n = 1;
+   t.max_size = h->cfg.max_size; t.ncol = h->ncol;
+   t.lut = h->d_lut; t.lut_min = h->lut_min; t.lut_len = h->lut_len;
+   t.code = h->d_code; t.code_stride = h->code_stride; t.meta = h->d_meta; t.work = h->d_work;
+   t.best_key = h->d_key; t.counters = h->d_counters; t.status = h->d_status;
+   PredictArgs p{};
+   p.data = h->d_data; p.nlin = h->nlin; p.ncol = h->ncol; p.ld = h->ld;
+   p.code = h->d_code; p.meta = h->d_meta; p.prot = h->cfg.protected_fns ? 1 : 0; p.out = h->d_pred;
+   const int P = 128;
+   const size_t smem = evaluate_smem_bytes(h->code_stride, h->ncol, P, 0);
+   if (smem > 200 * 1024) return fail(h, PPI_ERR_UNSUPPORTED, "too many columns");
+   const int tiles = (h->nlin + P * kR - 1) / (P * kR);
+   const int grid = std::max(1, std::min(tiles, 4 * h->sm_count));
+   PPI_CUDA(h, cudaEventRecord(h->ev0, h->stream));
+   PPI_CUDA(h, launch_translate(t, h->stream));
+   PPI_CUDA(h, launch_predict(h->cfg.math, p, P, grid, smem, h->stream));
+   PPI_CUDA(h, cudaEventRecord(h->ev1, h->stream));
+   PPI_CUDA(h, cudaMemcpyAsync(out, h->d_pred, (size_t)h->nlin * 4, cudaMemcpyDeviceToHost, h->stream));
+   PPI_CUDA(h, cudaStreamSynchronize(h->stream));
+   cudaEventElapsedTime(&h->last_ms, h->ev0, h->ev1);
+   h->last_launches = 2;
+   return PPI_OK;
+}
+
+ppi_status ppi_gpu_last_kernel_ms(ppi_gpu* h, float* ms) {
+   if (!h || !ms) return PPI_ERR_INVALID_ARGUMENT;
+   *ms = h->last_ms;
+   return PPI_OK;
+}
+
+int32_t ppi_gpu_last_launch_count(const ppi_gpu* h) { return h ? h->last_launches : 0; }
+
+ppi_status ppi_gpu_last_stage_ms(ppi_gpu* h, float* translate_ms, float* evaluate_ms) {
+   if (!h || !translate_ms || !evaluate_ms) return PPI_ERR_INVALID_ARGUMENT;
+   PPI_CUDA(h, cudaEventSynchronize(h->ev1));
+   PPI_CUDA(h, cudaEventElapsedTime(translate_ms, h->ev0, h->evm));
+   PPI_CUDA(h, cudaEventElapsedTime(evaluate_ms, h->evm, h->ev1));
+   return PPI_OK;
+}
+
+ppi_status ppi_gpu_set_grammar(ppi_gpu* h, const int32_t* rule_first, const int32_t* rule_count,
+                               int32_t n_nt, const int32_t* alt_len, const int32_t* alt_syms,
+                               int32_t n_alt, int32_t max_rule, int32_t t_const,
+                               int32_t t_attribute) {
+   if (!h) return PPI_ERR_INVALID_ARGUMENT;
+   if (!rule_first || !rule_count || !alt_len || !alt_syms || n_nt < 1 || n_alt < 1 ||
+       max_rule < 1)
+      return fail(h, PPI_ERR_INVALID_ARGUMENT, "bad grammar tables");
+   for (int i = 0; i < n_nt; ++i)
+      if (rule_count[i] < 1 || rule_first[i] < 0 || rule_first[i] + rule_count[i] > n_alt)
+         return fail(h, PPI_ERR_INVALID_ARGUMENT, "bad grammar tables");
+   for (int a = 0; a < n_alt; ++a) {
+      if (alt_len[a] < 1 || alt_len[a] > max_rule)
+         return fail(h, PPI_ERR_INVALID_ARGUMENT, "bad grammar tables");
+      for (int k = 0; k < alt_len[a]; ++k) {
+         const int s = alt_syms[(size_t)a * max_rule + k];
+         if (s < 10000 && (s < 0 || s >= n_nt))
+            return fail(h, PPI_ERR_INVALID_ARGUMENT, "grammar references an undefined non-terminal");
+      }
+   }
+   PPI_CUDA(h, cudaSetDevice(h->device));
+   free_decode_tables(&h->dec);
+   PPI_CUDA(h, upload_decode_tables(&h->dec, rule_first, rule_count, n_nt, alt_len, alt_syms,
+                                    n_alt, max_rule, t_const, t_attribute));
+   return PPI_OK;
+}
+
+static ppi_status decode_common(ppi_gpu* h, const uint8_t* genomes, int32_t n, int32_t nb,
+                                int32_t bg, int32_t bc) {
+   if (!h) return PPI_ERR_INVALID_ARGUMENT;
+   if (!h->dec.ready) return fail(h, PPI_ERR_NOT_READY, "no grammar: call ppi_gpu_set_grammar first");
+   if (h->pending) return fail(h, PPI_ERR_NOT_READY, "an evaluate_launch is still pending");
+   if (!genomes || n < 1 || n > h->cfg.population_size || nb < 1 || bg < 1 || bg > 31 || bc < 1 ||
+       bc > 63)
+      return fail(h, PPI_ERR_INVALID_ARGUMENT, "bad decode arguments");
+   PPI_CUDA(h, cudaSetDevice(h->device));
+   const size_t bytes = (size_t)n * nb;
+   if (bytes > h->genome_cap) {
+      cudaFree(h->d_genomes);
+      h->d_genomes = nullptr;
+      h->genome_cap = 0;
+      PPI_CUDA(h, dalloc(&h->d_genomes, bytes));
+      h->genome_cap = bytes;
+   }
+   const size_t frames = (size_t)n * (size_t)(nb / bg + 2);
+   if (frames > h->frames_cap) {
+      cudaFree(h->d_frames);
+      h->d_frames = nullptr;
+      h->frames_cap = 0;
+      PPI_CUDA(h, dalloc(&h->d_frames, frames));
+      h->frames_cap = frames;
+   }
+   PPI_CUDA(h, cudaMemcpyAsync(h->d_genomes, genomes, bytes, cudaMemcpyHostToDevice, h->stream));
+   return PPI_OK;
+}
+
+ppi_status ppi_gpu_decode(ppi_gpu* h, const uint8_t* genomes, int32_t n, int32_t nb, int32_t bg,
+                          int32_t bc, float lo, float hi, int32_t* phenotype, float* ephemeral,
+                          int32_t* size) {
+   ppi_status s = decode_common(h, genomes, n, nb, bg, bc);
+   if (s != PPI_OK) return s;
+   DecodeArgs d{};
+   d.t = h->dec; d.genomes = h->d_genomes; d.n = n; d.nb = nb; d.bg = bg; d.bc = bc; d.lo = lo;
+   d.hi = hi; d.max_size = h->cfg.max_size; d.phenotype = h->d_ph; d.ephemeral = h->d_eph;
+   d.size = h->d_size; d.frames = h->d_frames; d.frames_cap = nb / bg + 2;
+   PPI_CUDA(h, cudaEventRecord(h->ev0, h->stream));
+   PPI_CUDA(h, launch_decode(d, h->stream));
+   PPI_CUDA(h, cudaEventRecord(h->ev1, h->stream));
+   const size_t ms = (size_t)h->cfg.max_size;
+   if (phenotype)
+      PPI_CUDA(h, cudaMemcpyAsync(phenotype, h->d_ph, (size_t)n * ms * 4, cudaMemcpyDeviceToHost, h->stream));
+   if (ephemeral)
+      PPI_CUDA(h, cudaMemcpyAsync(ephemeral, h->d_eph, (size_t)n * ms * 4, cudaMemcpyDeviceToHost, h->stream));
+   if (size)
+      PPI_CUDA(h, cudaMemcpyAsync(size, h->d_size, (size_t)n * 4, cudaMemcpyDeviceToHost, h->stream));
+   PPI_CUDA(h, cudaStreamSynchronize(h->stream));
+   cudaEventElapsedTime(&h->last_ms, h->ev0, h->ev1);
+   h->last_launches = 1;
+   return PPI_OK;
+}
+
+ppi_status ppi_gpu_decode_evaluate(ppi_gpu* h, const uint8_t* genomes, int32_t n, int32_t nb,
+                                   int32_t bg, int32_t bc, float lo, float hi, float alpha,
+                                   float* fitness, int32_t* best_index, int32_t* size) {
+   ppi_status s = check_ready(h, n);
+   if (s != PPI_OK) return s;
+   if (!fitness) return fail(h, PPI_ERR_INVALID_ARGUMENT, "null fitness");
+   s = decode_common(h, genomes, n, nb, bg, bc);
+   if (s != PPI_OK) return s;
+   DecodeArgs d{};
+   d.t = h->dec; d.genomes = h->d_genomes; d.n = n; d.nb = nb; d.bg = bg; d.bc = bc; d.lo = lo;
+   d.hi = hi; d.max_size = h->cfg.max_size; d.phenotype = h->d_ph; d.ephemeral = h->d_eph;
+   d.size = h->d_size; d.frames = h->d_frames; d.frames_cap = nb / bg + 2;
+   PPI_CUDA(h, launch_decode(d, h->stream));
+   s = enqueue(h, h->d_ph, h->d_eph, h->d_size, n, alpha, h->d_fit, h->d_best, h->stream);
+   if (s != PPI_OK) return s;
+   h->last_launches = 3;
+   PPI_CUDA(h, cudaMemcpyAsync(h->h_fit, h->d_fit, (size_t)n * 4, cudaMemcpyDeviceToHost, h->stream));
+   PPI_CUDA(h, cudaMemcpyAsync(h->h_best, h->d_best, 4, cudaMemcpyDeviceToHost, h->stream));
+   PPI_CUDA(h, cudaMemcpyAsync(h->h_status, h->d_status, 4, cudaMemcpyDeviceToHost, h->stream));
+   if (size)
+      PPI_CUDA(h, cudaMemcpyAsync(size, h->d_size, (size_t)n * 4, cudaMemcpyDeviceToHost, h->stream));
+   PPI_CUDA(h, cudaStreamSynchronize(h->stream));
+   std::memcpy(fitness, h->h_fit, (size_t)n * sizeof(float));
+   if (best_index) *best_index = *h->h_best;
+   cudaEventElapsedTime(&h->last_ms, h->ev0, h->ev1);
+   if (*h->h_status & kStatusUnsupportedProgram)
+      return fail(h, PPI_ERR_UNSUPPORTED, "a program needs a deeper stack than supported");
+   return PPI_OK;
+}
+
+}  // extern "C"

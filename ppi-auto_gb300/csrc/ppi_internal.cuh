@@ -1,0 +1,296 @@
+// ppi_internal.cuh -- shared definitions of the GB300 evaluator: the
+// accumulator-machine bytecode that the translator emits and the evaluator
+// runs, per-opcode arithmetic in the three math modes, and kernel arguments.
+#pragma once
+
+#include <cstdint>
+#include <cfloat>
+#include <cuda_runtime.h>
+
+#include "ppi_gpu.h"
+
+namespace ppi {
+
+// Records each thread evaluates per bytecode instruction (register ILP).
+constexpr int kR = 8;
+// Register slots of the accumulator machine: a well-formed program whose
+// Sethi-Ullman number (with leaf operands folded into the instruction) is at
+// most kSlots runs on the register path.  Every binary tree of at most 255
+// nodes fits in 6 slots.
+constexpr int kSlots = 6;
+// Largest lane count (PDP work-items per program, DP records per group).
+constexpr int kMaxLanes = 4096;
+// Stack depth of the generic (stack) interpreter used for malformed programs
+// and programs needing more than kSlots slots.
+constexpr int kGenericStack = 128;
+// Column stride of the device dataset is a multiple of this.
+constexpr int kColumnPad = 1024;
+
+// Program kinds written by the translator.
+enum : int { kKindInvalid = 0, kKindFast = 1, kKindGeneric = 2, kKindUnsupported = 3 };
+
+// Status bits reported by the kernels.
+enum : int { kStatusUnsupportedProgram = 1 };
+
+// Accumulator-machine instructions.  Each is a uint2: .x = instruction id
+// below, .y = immediate (float bits of a constant, or a column index).
+//   acc, b, c : registers holding kR record values
+//   slot[s]   : kSlots register slots
+enum : uint32_t {
+   M_END = 0,
+   M_LDX_A = 1,   // acc = x[col]
+   M_LDC_A = 2,   // acc = imm
+   M_LDX_B = 3,   // b = x[col]
+   M_LDC_B = 4,   // b = imm
+   M_PUSH = 5,                      // + s : slot[s] = acc
+   M_FETCHB = M_PUSH + kSlots,      // + s : b = slot[s]
+   M_FETCHC = M_FETCHB + kSlots,    // + s : c = slot[s]
+   M_UN = M_FETCHC + kSlots,        // + (op - PPI_OP_NOT)  : acc = op(acc)
+   M_BB_L = M_UN + 25,              // + (op - PPI_OP_AND)  : acc = op(acc, b)
+   M_BB_R = M_BB_L + 18,            //                        acc = op(b, acc)
+   M_BC_L = M_BB_R + 18,            //                        acc = op(acc, imm)
+   M_BC_R = M_BC_L + 18,            //                        acc = op(imm, acc)
+   M_BX_L = M_BC_R + 18,            //                        acc = op(acc, x[col])
+   M_BX_R = M_BX_L + 18,            //                        acc = op(x[col], acc)
+   M_ITE = M_BX_R + 18,             // + perm: roles of (acc, b, c) as (cond, then, else)
+   M_COUNT = M_ITE + 6
+};
+static_assert(PPI_OP_TAN - PPI_OP_NOT + 1 == 25, "unary op count");
+static_assert(PPI_OP_DIV - PPI_OP_AND + 1 == 18, "binary op count");
+
+// ITE permutations: perm p -> register (0 = acc, 1 = b, 2 = c) holding
+// cond, then, else.
+__host__ __device__ constexpr int ite_role(int p, int role) {
+   constexpr int t[6][3] = {{0, 1, 2}, {0, 2, 1}, {1, 0, 2}, {1, 2, 0}, {2, 0, 1}, {2, 1, 0}};
+   return t[p][role];
+}
+
+__host__ __device__ inline int op_arity(int op) {
+   if (op == PPI_OP_IF_THEN_ELSE) return 3;
+   if (op >= PPI_OP_AND && op <= PPI_OP_DIV) return 2;
+   if (op >= PPI_OP_NOT && op < PPI_OP_COUNT) return 1;
+   return 0;
+}
+
+// ---------------------------------------------------------------------------
+// Arithmetic.  The whole library is compiled with -fmad=false, so no
+// multiply-add is contracted (the reference's host compiler does not contract
+// either on x86-64).  Float constants of src/interpreter/functions.h:19-57.
+constexpr float kPiF = 3.14159274101257f;
+constexpr float kPi2F = 1.57079637050629f;
+constexpr float kEF = 2.71828174591064f;
+
+enum : int { kMathFast = PPI_MATH_FAST, kMathParity = PPI_MATH_PARITY, kMathNative = PPI_MATH_NATIVE };
+
+template <int MATH> __device__ __forceinline__ float f_sin(float x) {
+   if constexpr (MATH == kMathParity) return (float)sin((double)x);
+   else if constexpr (MATH == kMathNative) return __sinf(x);
+   else return sinf(x);
+}
+template <int MATH> __device__ __forceinline__ float f_cos(float x) {
+   if constexpr (MATH == kMathParity) return (float)cos((double)x);
+   else if constexpr (MATH == kMathNative) return __cosf(x);
+   else return cosf(x);
+}
+template <int MATH> __device__ __forceinline__ float f_tan(float x) {
+   if constexpr (MATH == kMathParity) return (float)tan((double)x);
+   else if constexpr (MATH == kMathNative) return __tanf(x);
+   else return tanf(x);
+}
+template <int MATH> __device__ __forceinline__ float f_exp(float x) {
+   if constexpr (MATH == kMathParity) return (float)exp((double)x);
+   else if constexpr (MATH == kMathNative) return __expf(x);
+   else return expf(x);
+}
+template <int MATH> __device__ __forceinline__ float f_exp2(float x) {
+   if constexpr (MATH == kMathParity) return (float)exp2((double)x);
+   else return exp2f(x);
+}
+template <int MATH> __device__ __forceinline__ float f_exp10(float x) {
+   if constexpr (MATH == kMathParity) return (float)exp10((double)x);
+   else if constexpr (MATH == kMathNative) return __exp10f(x);
+   else return exp10f(x);
+}
+template <int MATH> __device__ __forceinline__ float f_log(float x) {
+   if constexpr (MATH == kMathParity) return (float)log((double)x);
+   else if constexpr (MATH == kMathNative) return __logf(x);
+   else return logf(x);
+}
+template <int MATH> __device__ __forceinline__ float f_log2(float x) {
+   if constexpr (MATH == kMathParity) return (float)log2((double)x);
+   else if constexpr (MATH == kMathNative) return __log2f(x);
+   else return log2f(x);
+}
+template <int MATH> __device__ __forceinline__ float f_log10(float x) {
+   if constexpr (MATH == kMathParity) return (float)log10((double)x);
+   else if constexpr (MATH == kMathNative) return __log10f(x);
+   else return log10f(x);
+}
+template <int MATH> __device__ __forceinline__ float f_pow(float a, float b) {
+   if constexpr (MATH == kMathParity) return (float)pow((double)a, (double)b);
+   else if constexpr (MATH == kMathNative) return __powf(a, b);
+   else return powf(a, b);
+}
+
+// Protected forms (src/interpreter/functions.h:99-193).
+__device__ __forceinline__ float p_sqrt(float x, int prot) {
+   float r = sqrtf(x);   // correctly rounded: equals (float)sqrt((double)x)
+   return (prot && x < 0.0f) ? 1.0f : r;
+}
+template <int MATH> __device__ __forceinline__ float p_div(float x, float y, int prot) {
+   float r;
+   if constexpr (MATH == kMathNative) r = __fdividef(x, y);
+   else r = x / y;
+   return (prot && y == 0.0f) ? 1.0f : r;
+}
+
+// T_GAMMA (interpreter_core:127-129).  PARITY follows sequential.cc, where
+// sinh and pow are double functions so x*sinh(...) and pow(...)*SQRT(...) are
+// double expressions; the other modes follow the all-float OpenCL kernel.
+template <int MATH> __device__ __forceinline__ float f_gamma(float x, int prot) {
+   if constexpr (MATH == kMathParity) {
+      double s = sinh((double)(1.0f / x));
+      float a = (x / kEF) * p_sqrt((float)((double)x * s), prot);
+      double p = pow((double)a, (double)x);
+      return (float)(p * (double)p_sqrt(2.0f * kPiF / x, prot));
+   } else {
+      float a = (x / kEF) * p_sqrt(x * sinhf(1.0f / x), prot);
+      return powf(a, x) * p_sqrt(2.0f * kPiF / x, prot);
+   }
+}
+
+__device__ __forceinline__ bool truthy(float v) { return v != 0.0f; }   // (bool)float
+
+template <int OP, int MATH> __device__ __forceinline__ float unop(float a, int prot) {
+   if constexpr (OP == PPI_OP_NOT) return truthy(a) ? 0.0f : 1.0f;
+   else if constexpr (OP == PPI_OP_ABS) return fabsf(a);
+   else if constexpr (OP == PPI_OP_POW2) return a * a;
+   else if constexpr (OP == PPI_OP_POW3) return (a * a) * a;
+   else if constexpr (OP == PPI_OP_POW4) return ((a * a) * a) * a;
+   else if constexpr (OP == PPI_OP_POW5) return (((a * a) * a) * a) * a;
+   else if constexpr (OP == PPI_OP_NEG) return -a;
+   else if constexpr (OP == PPI_OP_ROUND) return roundf(a);
+   else if constexpr (OP == PPI_OP_CEIL) return ceilf(a);
+   else if constexpr (OP == PPI_OP_FLOOR) return floorf(a);
+   else if constexpr (OP == PPI_OP_EXP) return f_exp<MATH>(a);
+   else if constexpr (OP == PPI_OP_EXP10) return f_exp10<MATH>(a);
+   else if constexpr (OP == PPI_OP_EXP2) return f_exp2<MATH>(a);
+   else if constexpr (OP == PPI_OP_SIN) return f_sin<MATH>(a);
+   else if constexpr (OP == PPI_OP_COS) return f_cos<MATH>(a);
+   else if constexpr (OP == PPI_OP_STEP) return (a >= 0.0f) ? 1.0f : 0.0f;
+   else if constexpr (OP == PPI_OP_SIGN) return a > 0.0f ? 1.0f : (a < 0.0f ? -1.0f : 0.0f);
+   else if constexpr (OP == PPI_OP_LOGISTIC) return 1.0f / (1.0f + f_exp<MATH>(-a));
+   else if constexpr (OP == PPI_OP_GAMMA) return f_gamma<MATH>(a, prot);
+   else if constexpr (OP == PPI_OP_GAUSS) return f_exp<MATH>(-a * a);
+   else if constexpr (OP == PPI_OP_SQRT) return p_sqrt(a, prot);
+   else if constexpr (OP == PPI_OP_LOG) { float r = f_log<MATH>(a); return (prot && a < 1.0f) ? 1.0f : r; }
+   else if constexpr (OP == PPI_OP_LOG10) { float r = f_log10<MATH>(a); return (prot && a < 1.0f) ? 1.0f : r; }
+   else if constexpr (OP == PPI_OP_LOG2) { float r = f_log2<MATH>(a); return (prot && a < 1.0f) ? 1.0f : r; }
+   else {
+      static_assert(OP == PPI_OP_TAN, "unary op");
+      float r = f_tan<MATH>(a);
+      const float fa = fabsf(a);
+      return (prot && (fa == kPi2F || fa == 3.0f * kPi2F)) ? 1.0f : r;
+   }
+}
+
+// a = stack[top] (left operand), b = stack[top-1] (right operand).
+template <int OP, int MATH> __device__ __forceinline__ float binop(float a, float b, int prot) {
+   if constexpr (OP == PPI_OP_AND) return (truthy(a) && truthy(b)) ? 1.0f : 0.0f;
+   else if constexpr (OP == PPI_OP_OR) return (truthy(a) || truthy(b)) ? 1.0f : 0.0f;
+   else if constexpr (OP == PPI_OP_XOR) return (truthy(a) != truthy(b)) ? 1.0f : 0.0f;
+   else if constexpr (OP == PPI_OP_GREATER) return (a > b) ? 1.0f : 0.0f;
+   else if constexpr (OP == PPI_OP_GREATEREQUAL) return (a >= b) ? 1.0f : 0.0f;
+   else if constexpr (OP == PPI_OP_LESS) return (a < b) ? 1.0f : 0.0f;
+   else if constexpr (OP == PPI_OP_LESSEQUAL) return (a <= b) ? 1.0f : 0.0f;
+   else if constexpr (OP == PPI_OP_EQUAL) return (a == b) ? 1.0f : 0.0f;
+   else if constexpr (OP == PPI_OP_NOTEQUAL) return (a != b) ? 1.0f : 0.0f;
+   else if constexpr (OP == PPI_OP_ADD) return a + b;
+   else if constexpr (OP == PPI_OP_SUB) return a - b;
+   else if constexpr (OP == PPI_OP_MULT) return a * b;
+   else if constexpr (OP == PPI_OP_MEAN) return (a + b) / 2.0f;
+   else if constexpr (OP == PPI_OP_MAX) return fmaxf(a, b);
+   else if constexpr (OP == PPI_OP_MIN) return fminf(a, b);
+   else if constexpr (OP == PPI_OP_MOD) return fmodf(a, b);
+   else if constexpr (OP == PPI_OP_POW) return f_pow<MATH>(a, b);
+   else {
+      static_assert(OP == PPI_OP_DIV, "binary op");
+      return p_div<MATH>(a, b, prot);
+   }
+}
+
+// ERROR(X,Y) (src/definitions.h:18); the COST form guarded as documented in
+// ppi_gpu.h.
+__device__ __forceinline__ float apply_error(int ef, float x, float y, const float* cost, int cn) {
+   switch (ef) {
+   case PPI_EF_ABS: return fabsf(x - y);
+   case PPI_EF_SQUARED: { float d = x - y; return d * d; }
+   case PPI_EF_MISCLASS: return (x != y) ? 1.0f : 0.0f;
+   default: {
+      if (x != x) return x;
+      const float fn = (float)cn;
+      int ix = x >= fn ? cn - 1 : (x > 0.0f ? (int)x : 0);
+      int iy = y != y ? 0 : (y >= fn ? cn - 1 : (y > 0.0f ? (int)y : 0));
+      return __ldg(cost + ix * cn + iy);
+   }
+   }
+}
+
+__device__ __forceinline__ bool nonfinite(float v) { return isinf(v) || isnan(v); }
+
+// ---------------------------------------------------------------------------
+struct TranslateArgs {
+   const int32_t* phenotype;   // program i at phenotype + i * max_size
+   const float* ephemeral;
+   const int32_t* size;
+   int n, max_size, ncol;
+   const int2* lut;            // lut[sym - lut_min] = {op, literal bits}
+   int lut_min, lut_len;
+   uint2* code;                // program i at code + i * code_stride
+   int code_stride;
+   int2* meta;                 // {kind, code length}
+   uint2* work;                // translator scratch: n x max_size
+   unsigned long long* best_key;
+   unsigned* counters;         // [0] work queue, [1] finished blocks
+   int* status;
+};
+
+struct EvalArgs {
+   const float* data;          // column-major, column c at data + c * ld
+   int nlin, ncol, ld;
+   const uint2* code;
+   int code_stride;
+   const int2* meta;
+   const int32_t* size;
+   int n;
+   float alpha;
+   int ef, reduce_max, prot;
+   const float* cost;
+   int cost_n;
+   int strategy, lanes;
+   float* fitness;
+   unsigned long long* best_key;
+   unsigned* counters;
+   int32_t* best_index;
+   int* status;
+};
+
+struct PredictArgs {
+   const float* data;
+   int nlin, ncol, ld;
+   const uint2* code;
+   const int2* meta;
+   int prot;
+   float* out;
+};
+
+// Kernel launchers (evaluate.cu / translate.cu).
+cudaError_t launch_translate(const TranslateArgs& a, cudaStream_t s);
+cudaError_t launch_evaluate(int math, const EvalArgs& a, int block, int grid, size_t smem,
+                            cudaStream_t s);
+cudaError_t launch_predict(int math, const PredictArgs& a, int block, int grid, size_t smem,
+                           cudaStream_t s);
+cudaError_t evaluate_occupancy(int math, int block, size_t smem, int* blocks_per_sm);
+size_t evaluate_smem_bytes(int code_stride, int ncol, int block, int lanes);
+
+}  // namespace ppi

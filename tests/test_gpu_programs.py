@@ -1,0 +1,147 @@
+"""Program shapes that exercise every path of the GPU evaluator: all register
+slots, every ITE permutation, leaf folding on either side, the generic stack
+interpreter (register need above 6, malformed programs), invalid attribute
+indices, unknown symbols, size 0 / size > max_size, lane counts that do not
+divide the records, one record, and tiny populations."""
+import numpy as np
+import pytest
+
+from helpers import ProgramGen, assert_bitexact, load_golden, make_evaluator, oracle_for
+
+pytestmark = pytest.mark.gpu
+
+
+def _dataset(rng, nlin, nfeat, ef="abs"):
+    X = rng.normal(0, 2, (nlin, nfeat)).astype(np.float32)
+    y = (rng.integers(0, 3, nlin) if ef == "misclass" else rng.normal(0, 2, nlin)).astype(np.float32)
+    return np.concatenate([X, y[:, None]], 1)
+
+
+def _check(oracle_lib, d, rows, ph, ep, sz, strat, lanes, math="parity", alpha=1e-6):
+    ev = make_evaluator(d, strat, lanes, math, population=len(sz), max_size=ph.shape[1], rows=rows)
+    f, best = ev.evaluate(ph, ep, sz, alpha)
+    L = 1 if strat == "PP" else (lanes if lanes > 0 else min(len(rows), 1024))
+    ref = oracle_for(oracle_lib, d, rows=rows).evaluate(ph, ep, sz, strat, L, alpha)
+    assert_bitexact(f, ref, "%s%d" % (strat, lanes))
+    assert best == oracle_lib.best_index(ref)
+    return f
+
+
+@pytest.mark.parametrize("fixture", ["allops", "allops_prot", "allops_sqmax", "cfg5", "random"])
+@pytest.mark.parametrize("strat,lanes", [("PDP", 0), ("PP", 0), ("DP", 48), ("PDP", 100)])
+def test_random_trees(gpu_lib, oracle_lib, fixture, strat, lanes):
+    d = load_golden(fixture)
+    rng = np.random.default_rng(hash((fixture, strat, lanes)) % 2**32)
+    rows = _dataset(rng, 777, d["rows"].shape[1] - 1, d["ef"])
+    gen = ProgramGen(d, rng, rows.shape[1])
+    progs = [gen.random(int(k)) for k in rng.integers(0, 60, 150)]
+    progs += [gen.full(k) for k in range(1, 8)]            # need 0..6: every slot
+    progs += [gen.full(8)[:255]]                           # truncated: malformed, generic path
+    ph, ep, sz = ProgramGen.rows(progs, 256)
+    _check(oracle_lib, d, rows, ph, ep, sz, strat, lanes)
+
+
+def test_register_need_above_slots_uses_generic_path(gpu_lib, oracle_lib):
+    d = load_golden("allops")
+    rng = np.random.default_rng(3)
+    rows = _dataset(rng, 300, 3)
+    gen = ProgramGen(d, rng, rows.shape[1])
+    progs = [gen.full(8), gen.full(7), gen.full(6)]         # need 7 (generic), 6, 5
+    ph, ep, sz = ProgramGen.rows(progs, 511)
+    _check(oracle_lib, d, rows, ph, ep, sz, "PDP", 0)
+
+
+def test_ite_all_permutations(gpu_lib, oracle_lib):
+    d = load_golden("allops")
+    rng = np.random.default_rng(4)
+    rows = _dataset(rng, 500, 3)
+    gen = ProgramGen(d, rng, rows.shape[1])
+    ite = (gen.by_op[gen.G.OP["IF_THEN_ELSE"]][0], 0.0)
+    progs = []
+    for a in range(4):
+        for b in range(4):
+            for c in range(4):
+                progs.append([ite] + gen.full(a) + gen.full(b) + gen.full(c))
+    ph, ep, sz = ProgramGen.rows(progs, 64)
+    _check(oracle_lib, d, rows, ph, ep, sz, "PDP", 0)
+
+
+def test_malformed_invalid_and_edge_programs(gpu_lib, oracle_lib):
+    d = load_golden("allops")
+    rng = np.random.default_rng(5)
+    rows = _dataset(rng, 130, 3)
+    gen = ProgramGen(d, rng, rows.shape[1])
+    G = gen.G
+    attr = gen.by_op[G.OP["ATTRIBUTE"]][0]
+    add = gen.by_op[G.OP["ADD"]][0]
+    sin = gen.by_op[G.OP["SIN"]][0]
+    progs = [
+        [(add, 0.0)],                                  # binary with no operands
+        [(add, 0.0), (attr, 0.0)],                     # one operand missing
+        [(attr, 0.0), (attr, 1.0)],                    # two values left (forest)
+        [(sin, 0.0)],                                  # unary with no operand
+        [(attr, 7.0)],                                 # attribute index past ncol
+        [(attr, -1.0)],                                # negative attribute index
+        [(attr, float("nan"))],
+        [(987654, 0.0)],                               # symbol outside the table
+        [(add, 0.0), (987654, 0.0), (attr, 2.0)],
+        [(attr, 3.0)],                                 # reads the target column
+    ]
+    ph, ep, sz = ProgramGen.rows(progs, 8)
+    sz = np.concatenate([sz, [0, 9, -3]]).astype(np.int32)   # size 0, > max_size, negative
+    ph = np.concatenate([ph, np.zeros((3, 8), np.int32)])
+    ep = np.concatenate([ep, np.zeros((3, 8), np.float32)])
+    for strat, lanes in [("PDP", 0), ("PP", 0), ("DP", 16), ("DP", 1000)]:
+        _check(oracle_lib, d, rows, ph, ep, sz, strat, lanes)
+
+
+@pytest.mark.parametrize("nlin", [1, 2, 31, 1023, 1024, 1025, 2049])
+@pytest.mark.parametrize("strat,lanes", [("PDP", 0), ("PP", 0), ("DP", 0), ("PDP", 3)])
+def test_record_counts(gpu_lib, oracle_lib, nlin, strat, lanes):
+    d = load_golden("cfg2")
+    rng = np.random.default_rng(nlin)
+    rows = _dataset(rng, nlin, 1)
+    gen = ProgramGen(d, rng, rows.shape[1])
+    progs = [gen.random(int(k)) for k in rng.integers(0, 40, 37)]
+    ph, ep, sz = ProgramGen.rows(progs, 128)
+    _check(oracle_lib, d, rows, ph, ep, sz, strat, lanes)
+
+
+def test_population_of_one_and_all_invalid(gpu_lib, oracle_lib):
+    d = load_golden("cfg2")
+    rng = np.random.default_rng(9)
+    rows = _dataset(rng, 200, 1)
+    ph = np.zeros((3, 16), np.int32)
+    ep = np.zeros((3, 16), np.float32)
+    sz = np.zeros(3, np.int32)
+    f = _check(oracle_lib, d, rows, ph, ep, sz, "PDP", 0)
+    assert (f == np.float32(3.4028235e38)).all()
+    gen = ProgramGen(d, rng, rows.shape[1])
+    ph, ep, sz = ProgramGen.rows([gen.random(5)], 16)
+    _check(oracle_lib, d, rows, ph, ep, sz, "PP", 0)
+
+
+def test_misclassification_and_reducemax_bitexact_in_fast_math(gpu_lib, oracle_lib):
+    """Counts and maxima are order-independent: with the same per-record
+    predictions fast math must reproduce them exactly.  Programs without
+    transcendental ops have identical predictions in every math mode."""
+    d = load_golden("cfg1")
+    rng = np.random.default_rng(11)
+    rows = d["rows"]
+    gen = ProgramGen(d, rng, rows.shape[1])
+    G = gen.G
+    gen.un = []                                   # + - * / only
+    gen.bi = [G.OP["ADD"], G.OP["SUB"], G.OP["MULT"], G.OP["DIV"]]
+    progs = [gen.random(int(k)) for k in rng.integers(0, 30, 80)]
+    ph, ep, sz = ProgramGen.rows(progs, 64)
+    _check(oracle_lib, d, rows, ph, ep, sz, "PDP", 0, math="fast")
+
+    dm = load_golden("cfg2max")
+    rng = np.random.default_rng(12)
+    gen = ProgramGen(dm, rng, dm["rows"].shape[1])
+    gen.un = []
+    gen.bi = [G.OP["ADD"], G.OP["SUB"], G.OP["MULT"], G.OP["DIV"]]
+    progs = [gen.random(int(k)) for k in rng.integers(0, 30, 80)]
+    ph, ep, sz = ProgramGen.rows(progs, 128)
+    for strat in ("DP", "PDP", "PP"):
+        _check(oracle_lib, dm, dm["rows"], ph, ep, sz, strat, 0, math="fast")
