@@ -179,7 +179,7 @@ def run_ours(args):
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
-    wl = workloads.polynomial(seed=1234 + rank)
+    wl = workloads.polynomial(seed=1234 + rank, nlin=args.records, population=args.population)
     ev = ppi_gpu.Evaluator(wl.grammar.symbol_table_arrays(), wl.max_size, wl.population,
                            wl.strategy, 0, wl.error_fn, wl.cost, wl.reduce_max, wl.protected,
                            args.math, device=local)
@@ -309,6 +309,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--math", default="fast", choices=["fast", "parity", "native"])
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    # smaller cases of the same workload, for profiling captures only
+    ap.add_argument("--records", type=int, default=100_000)
+    ap.add_argument("--population", type=int, default=30_000)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
     if args.impl == "reference":

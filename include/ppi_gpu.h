@@ -195,6 +195,10 @@ ppi_status ppi_gpu_last_kernel_ms(ppi_gpu* h, float* ms);
  * evaluate call (it waits for that call's work to finish). */
 ppi_status ppi_gpu_last_stage_ms(ppi_gpu* h, float* translate_ms, float* evaluate_ms);
 
+/* Lane count in use (PDP work-items per program, DP records per group, 1 for
+ * PP), resolved by ppi_gpu_set_dataset; 0 before a dataset is set. */
+int32_t ppi_gpu_lanes(const ppi_gpu* h);
+
 /* Number of kernel launches the last evaluate / predict / decode call made. */
 int32_t ppi_gpu_last_launch_count(const ppi_gpu* h);
 

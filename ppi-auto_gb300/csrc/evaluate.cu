@@ -29,60 +29,38 @@ __device__ __forceinline__ size_t code_bytes(int code_stride) {
    return ((size_t)(code_stride + 1) * sizeof(uint2) + 15) & ~(size_t)15;
 }
 
-__device__ __forceinline__ void load_x(const float* tile, uint32_t col, int T, int tid, float (&x)[kR]) {
-   const float4* p = reinterpret_cast<const float4*>(tile + (size_t)col * T + tid * kR);
-   const float4 u = p[0], v = p[1];
+__device__ __forceinline__ void load_row(const float* p, float (&x)[kR]) {
+   const float4* q = reinterpret_cast<const float4*>(p);
+   const float4 u = q[0], v = q[1];
    x[0] = u.x; x[1] = u.y; x[2] = u.z; x[3] = u.w;
    x[4] = v.x; x[5] = v.y; x[6] = v.z; x[7] = v.w;
 }
-static_assert(kR == 8, "load_x assumes 8 records per thread");
+__device__ __forceinline__ void store_row(float* p, const float (&x)[kR]) {
+   float4* q = reinterpret_cast<float4*>(p);
+   q[0] = make_float4(x[0], x[1], x[2], x[3]);
+   q[1] = make_float4(x[4], x[5], x[6], x[7]);
+}
+static_assert(kR == 8, "load_row assumes 8 records per thread");
 
-// ---- register path ----------------------------------------------------------
+// ---- bytecode path -------------------------------------------------------------
+// `mine` points at this thread's kR positions of row 0; row k is at mine + k*T.
 template <int MATH>
-__device__ __forceinline__ void run_fast(const uint2* __restrict__ code, const float* __restrict__ tile,
-                                         int T, int tid, float (&acc)[kR], int prot) {
-   float b[kR], c[kR], slot[kSlots][kR];
-#pragma unroll
-   for (int r = 0; r < kR; ++r) { acc[r] = 0.0f; b[r] = 0.0f; c[r] = 0.0f; }
-#pragma unroll
-   for (int s = 0; s < kSlots; ++s)
-#pragma unroll
-      for (int r = 0; r < kR; ++r) slot[s][r] = 0.0f;
-
+__device__ __forceinline__ void run_fast(const uint2* __restrict__ code, float* mine, int T,
+                                         float (&acc)[kR], int prot) {
    int pc = 0;
    uint2 ins = code[0];
    for (;;) {
       const uint2 nxt = code[pc + 1];
       switch (ins.x) {
       case M_END: return;
-      case M_LDX_A: load_x(tile, ins.y, T, tid, acc); break;
-      case M_LDC_A: {
+      case M_LD_ROW: load_row(mine + (size_t)ins.y * T, acc); break;
+      case M_LD_C: {
          const float k = __uint_as_float(ins.y);
 #pragma unroll
          for (int r = 0; r < kR; ++r) acc[r] = k;
          break;
       }
-      case M_LDX_B: load_x(tile, ins.y, T, tid, b); break;
-      case M_LDC_B: {
-         const float k = __uint_as_float(ins.y);
-#pragma unroll
-         for (int r = 0; r < kR; ++r) b[r] = k;
-         break;
-      }
-#define PPI_SLOT_CASES(S)                                                          \
-      case M_PUSH + S:                                                             \
-         _Pragma("unroll") for (int r = 0; r < kR; ++r) slot[S][r] = acc[r];       \
-         break;                                                                    \
-      case M_FETCHB + S:                                                           \
-         _Pragma("unroll") for (int r = 0; r < kR; ++r) b[r] = slot[S][r];         \
-         break;                                                                    \
-      case M_FETCHC + S:                                                           \
-         _Pragma("unroll") for (int r = 0; r < kR; ++r) c[r] = slot[S][r];         \
-         break;
-      PPI_SLOT_CASES(0) PPI_SLOT_CASES(1) PPI_SLOT_CASES(2)
-      PPI_SLOT_CASES(3) PPI_SLOT_CASES(4) PPI_SLOT_CASES(5)
-#undef PPI_SLOT_CASES
-      static_assert(kSlots == 6, "slot cases");
+      case M_PUSH: store_row(mine + (size_t)ins.y * T, acc); break;
 
 #define PPI_UN_CASE(OP)                                                            \
       case M_UN + (OP - PPI_OP_NOT):                                               \
@@ -100,12 +78,18 @@ __device__ __forceinline__ void run_fast(const uint2* __restrict__ code, const f
 #undef PPI_UN_CASE
 
 #define PPI_BIN_CASES(OP)                                                          \
-      case M_BB_L + (OP - PPI_OP_AND):                                             \
-         _Pragma("unroll") for (int r = 0; r < kR; ++r) acc[r] = binop<OP, MATH>(acc[r], b[r], prot); \
+      case M_BR_L + (OP - PPI_OP_AND): {                                           \
+         float x[kR];                                                              \
+         load_row(mine + (size_t)ins.y * T, x);                                    \
+         _Pragma("unroll") for (int r = 0; r < kR; ++r) acc[r] = binop<OP, MATH>(acc[r], x[r], prot); \
          break;                                                                    \
-      case M_BB_R + (OP - PPI_OP_AND):                                             \
-         _Pragma("unroll") for (int r = 0; r < kR; ++r) acc[r] = binop<OP, MATH>(b[r], acc[r], prot); \
+      }                                                                            \
+      case M_BR_R + (OP - PPI_OP_AND): {                                           \
+         float x[kR];                                                              \
+         load_row(mine + (size_t)ins.y * T, x);                                    \
+         _Pragma("unroll") for (int r = 0; r < kR; ++r) acc[r] = binop<OP, MATH>(x[r], acc[r], prot); \
          break;                                                                    \
+      }                                                                            \
       case M_BC_L + (OP - PPI_OP_AND): {                                           \
          const float k = __uint_as_float(ins.y);                                   \
          _Pragma("unroll") for (int r = 0; r < kR; ++r) acc[r] = binop<OP, MATH>(acc[r], k, prot); \
@@ -114,18 +98,6 @@ __device__ __forceinline__ void run_fast(const uint2* __restrict__ code, const f
       case M_BC_R + (OP - PPI_OP_AND): {                                           \
          const float k = __uint_as_float(ins.y);                                   \
          _Pragma("unroll") for (int r = 0; r < kR; ++r) acc[r] = binop<OP, MATH>(k, acc[r], prot); \
-         break;                                                                    \
-      }                                                                            \
-      case M_BX_L + (OP - PPI_OP_AND): {                                           \
-         float x[kR];                                                              \
-         load_x(tile, ins.y, T, tid, x);                                           \
-         _Pragma("unroll") for (int r = 0; r < kR; ++r) acc[r] = binop<OP, MATH>(acc[r], x[r], prot); \
-         break;                                                                    \
-      }                                                                            \
-      case M_BX_R + (OP - PPI_OP_AND): {                                           \
-         float x[kR];                                                              \
-         load_x(tile, ins.y, T, tid, x);                                           \
-         _Pragma("unroll") for (int r = 0; r < kR; ++r) acc[r] = binop<OP, MATH>(x[r], acc[r], prot); \
          break;                                                                    \
       }
       PPI_BIN_CASES(PPI_OP_AND) PPI_BIN_CASES(PPI_OP_OR) PPI_BIN_CASES(PPI_OP_XOR)
@@ -138,12 +110,16 @@ __device__ __forceinline__ void run_fast(const uint2* __restrict__ code, const f
 #undef PPI_BIN_CASES
 
 #define PPI_ITE_CASE(P)                                                            \
-      case M_ITE + P:                                                              \
+      case M_ITE + P: {                                                            \
+         float ra[kR], rb[kR];                                                     \
+         load_row(mine + (size_t)(ins.y & 0xFFFFu) * T, ra);                       \
+         load_row(mine + (size_t)(ins.y >> 16) * T, rb);                           \
          _Pragma("unroll") for (int r = 0; r < kR; ++r) {                          \
-            const float v3[3] = {acc[r], b[r], c[r]};                              \
+            const float v3[3] = {acc[r], ra[r], rb[r]};                            \
             acc[r] = truthy(v3[ite_role(P, 0)]) ? v3[ite_role(P, 1)] : v3[ite_role(P, 2)]; \
          }                                                                         \
-         break;
+         break;                                                                    \
+      }
       PPI_ITE_CASE(0) PPI_ITE_CASE(1) PPI_ITE_CASE(2) PPI_ITE_CASE(3) PPI_ITE_CASE(4)
       PPI_ITE_CASE(5)
 #undef PPI_ITE_CASE
@@ -270,7 +246,7 @@ __global__ void __launch_bounds__(128, 4) eval_kernel(const EvalArgs a) {
    const int L = a.lanes;
    uint2* s_code = reinterpret_cast<uint2*>(smem_raw);
    float* s_tile = reinterpret_cast<float*>(smem_raw + code_bytes(a.code_stride));
-   float* s_err = s_tile + (size_t)a.ncol * T;
+   float* s_err = s_tile + (size_t)(a.ncol + kSlots) * T;
    float* s_acc = s_err + T;
    int* s_done = reinterpret_cast<int*>(s_acc + L);
    const bool aligned = a.strategy == PPI_STRATEGY_PDP && L == T;
@@ -315,7 +291,7 @@ __global__ void __launch_bounds__(128, 4) eval_kernel(const EvalArgs a) {
             __syncthreads();
             float v[kR];
             if (m.x == kKindFast) {
-               run_fast<MATH>(s_code, s_tile, T, tid, v, a.prot);
+               run_fast<MATH>(s_code, s_tile + tid * kR, T, v, a.prot);
             } else {
                float tmp[kR];
                run_generic<MATH>(s_code, s_tile, T, tid, tmp, a.prot);
@@ -436,7 +412,7 @@ __global__ void __launch_bounds__(128, 4) predict_kernel(const PredictArgs a) {
       __syncthreads();
       float v[kR];
       if (m.x == kKindFast) {
-         run_fast<MATH>(s_code, s_tile, T, tid, v, a.prot);
+         run_fast<MATH>(s_code, s_tile + tid * kR, T, v, a.prot);
       } else if (m.x == kKindGeneric) {
          float tmp[kR];
          run_generic<MATH>(s_code, s_tile, T, tid, tmp, a.prot);
@@ -483,7 +459,7 @@ cudaError_t launch_predict_t(const PredictArgs& a, int block, int grid, size_t s
 size_t evaluate_smem_bytes(int code_stride, int ncol, int block, int lanes) {
    const size_t T = (size_t)block * kR;
    const size_t code = ((size_t)(code_stride + 1) * sizeof(uint2) + 15) & ~(size_t)15;
-   return code + (size_t)ncol * T * 4 + T * 4 + (size_t)lanes * 8;
+   return code + (size_t)(ncol + kSlots) * T * 4 + T * 4 + (size_t)lanes * 8;
 }
 
 cudaError_t launch_evaluate(int math, const EvalArgs& a, int block, int grid, size_t smem,

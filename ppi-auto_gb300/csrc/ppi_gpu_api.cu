@@ -371,8 +371,12 @@ ppi_status ppi_gpu_predict(ppi_gpu* h, const int32_t* ph, const float* eph, int3
    PredictArgs p{};
    p.data = h->d_data; p.nlin = h->nlin; p.ncol = h->ncol; p.ld = h->ld;
    p.code = h->d_code; p.meta = h->d_meta; p.prot = h->cfg.protected_fns ? 1 : 0; p.out = h->d_pred;
-   const int P = 128;
-   const size_t smem = evaluate_smem_bytes(h->code_stride, h->ncol, P, 0);
+   int P = 128;
+   size_t smem = evaluate_smem_bytes(h->code_stride, h->ncol, P, 0);
+   while (smem > 200 * 1024 && P > 32) {
+      P /= 2;
+      smem = evaluate_smem_bytes(h->code_stride, h->ncol, P, 0);
+   }
    if (smem > 200 * 1024) return fail(h, PPI_ERR_UNSUPPORTED, "too many columns");
    const int tiles = (h->nlin + P * kR - 1) / (P * kR);
    const int grid = std::max(1, std::min(tiles, 4 * h->sm_count));
@@ -394,6 +398,8 @@ ppi_status ppi_gpu_last_kernel_ms(ppi_gpu* h, float* ms) {
 }
 
 int32_t ppi_gpu_last_launch_count(const ppi_gpu* h) { return h ? h->last_launches : 0; }
+
+int32_t ppi_gpu_lanes(const ppi_gpu* h) { return (h && h->have_data) ? h->lanes : 0; }
 
 ppi_status ppi_gpu_last_stage_ms(ppi_gpu* h, float* translate_ms, float* evaluate_ms) {
    if (!h || !translate_ms || !evaluate_ms) return PPI_ERR_INVALID_ARGUMENT;

@@ -13,9 +13,9 @@ namespace ppi {
 
 // Records each thread evaluates per bytecode instruction (register ILP).
 constexpr int kR = 8;
-// Register slots of the accumulator machine: a well-formed program whose
+// Slot rows of the accumulator machine: a well-formed program whose
 // Sethi-Ullman number (with leaf operands folded into the instruction) is at
-// most kSlots runs on the register path.  Every binary tree of at most 255
+// most kSlots runs on the bytecode path.  Every binary tree of at most 255
 // nodes fits in 6 slots.
 constexpr int kSlots = 6;
 // Largest lane count (PDP work-items per program, DP records per group).
@@ -33,33 +33,31 @@ enum : int { kKindInvalid = 0, kKindFast = 1, kKindGeneric = 2, kKindUnsupported
 enum : int { kStatusUnsupportedProgram = 1 };
 
 // Accumulator-machine instructions.  Each is a uint2: .x = instruction id
-// below, .y = immediate (float bits of a constant, or a column index).
-//   acc, b, c : registers holding kR record values
-//   slot[s]   : kSlots register slots
+// below, .y = immediate: float bits of a constant, or a row index.
+// The only register state is `acc` (kR record values per thread).  Every
+// other operand is a "row" of the CTA's shared-memory tile: rows 0..ncol-1
+// hold the staged record columns, rows ncol..ncol+kSlots-1 are the slots
+// where a pending subexpression is parked.  Each thread reads and writes only
+// its own kR positions of a row.
 enum : uint32_t {
    M_END = 0,
-   M_LDX_A = 1,   // acc = x[col]
-   M_LDC_A = 2,   // acc = imm
-   M_LDX_B = 3,   // b = x[col]
-   M_LDC_B = 4,   // b = imm
-   M_PUSH = 5,                      // + s : slot[s] = acc
-   M_FETCHB = M_PUSH + kSlots,      // + s : b = slot[s]
-   M_FETCHC = M_FETCHB + kSlots,    // + s : c = slot[s]
-   M_UN = M_FETCHC + kSlots,        // + (op - PPI_OP_NOT)  : acc = op(acc)
-   M_BB_L = M_UN + 25,              // + (op - PPI_OP_AND)  : acc = op(acc, b)
-   M_BB_R = M_BB_L + 18,            //                        acc = op(b, acc)
-   M_BC_L = M_BB_R + 18,            //                        acc = op(acc, imm)
+   M_LD_ROW = 1,                    // acc = row[imm]
+   M_LD_C = 2,                      // acc = imm
+   M_PUSH = 3,                      // row[imm] = acc
+   M_UN = 4,                        // + (op - PPI_OP_NOT)  : acc = op(acc)
+   M_BR_L = M_UN + 25,              // + (op - PPI_OP_AND)  : acc = op(acc, row[imm])
+   M_BR_R = M_BR_L + 18,            //                        acc = op(row[imm], acc)
+   M_BC_L = M_BR_R + 18,            //                        acc = op(acc, imm)
    M_BC_R = M_BC_L + 18,            //                        acc = op(imm, acc)
-   M_BX_L = M_BC_R + 18,            //                        acc = op(acc, x[col])
-   M_BX_R = M_BX_L + 18,            //                        acc = op(x[col], acc)
-   M_ITE = M_BX_R + 18,             // + perm: roles of (acc, b, c) as (cond, then, else)
+   M_ITE = M_BC_R + 18,             // + perm: rows a = imm & 0xFFFF, b = imm >> 16;
+                                    //   roles of (acc, a, b) as (cond, then, else)
    M_COUNT = M_ITE + 6
 };
 static_assert(PPI_OP_TAN - PPI_OP_NOT + 1 == 25, "unary op count");
 static_assert(PPI_OP_DIV - PPI_OP_AND + 1 == 18, "binary op count");
 
-// ITE permutations: perm p -> register (0 = acc, 1 = b, 2 = c) holding
-// cond, then, else.
+// ITE permutations: perm p -> operand (0 = acc, 1 = row a, 2 = row b)
+// holding cond, then, else.
 __host__ __device__ constexpr int ite_role(int p, int role) {
    constexpr int t[6][3] = {{0, 1, 2}, {0, 2, 1}, {1, 0, 2}, {1, 2, 0}, {2, 0, 1}, {2, 1, 0}};
    return t[p][role];

@@ -128,6 +128,7 @@ __global__ void translate_kernel(const TranslateArgs a) {
       };
       auto is_leaf = [&](int node) { return op_arity(node_op(w[node])) == 0; };
       auto leaf_attr = [&](int node) { return node_op(w[node]) == PPI_OP_ATTRIBUTE; };
+      const uint32_t slot0 = (uint32_t)a.ncol;   // row of slot 0
       while (fp > 0) {
          const uint32_t f = frames[fp - 1];
          const int node = (int)(f & 0xFFFFu), d = (int)((f >> 16) & 0xFFu), st = (int)(f >> 24);
@@ -135,7 +136,7 @@ __global__ void translate_kernel(const TranslateArgs a) {
          const int op = node_op(wn);
          const int ar = op_arity(op);
          if (ar == 0) {
-            emit(op == PPI_OP_ATTRIBUTE ? M_LDX_A : M_LDC_A, wn.y);
+            emit(op == PPI_OP_ATTRIBUTE ? M_LD_ROW : M_LD_C, wn.y);
             --fp;
             continue;
          }
@@ -150,15 +151,15 @@ __global__ void translate_kernel(const TranslateArgs a) {
             const uint32_t bo = (uint32_t)(op - PPI_OP_AND);
             const bool l0 = is_leaf(c0), l1 = is_leaf(c1);
             if (l0 && l1) {
-               emit(leaf_attr(c0) ? M_LDX_A : M_LDC_A, w[c0].y);
-               emit((leaf_attr(c1) ? M_BX_L : M_BC_L) + bo, w[c1].y);
+               emit(leaf_attr(c0) ? M_LD_ROW : M_LD_C, w[c0].y);
+               emit((leaf_attr(c1) ? M_BR_L : M_BC_L) + bo, w[c1].y);
                --fp;
             } else if (l1) {
                if (st == 0) { frames[fp - 1] = frame(node, d, 1); frames[fp++] = frame(c0, d, 0); }
-               else { emit((leaf_attr(c1) ? M_BX_L : M_BC_L) + bo, w[c1].y); --fp; }
+               else { emit((leaf_attr(c1) ? M_BR_L : M_BC_L) + bo, w[c1].y); --fp; }
             } else if (l0) {
                if (st == 0) { frames[fp - 1] = frame(node, d, 1); frames[fp++] = frame(c1, d, 0); }
-               else { emit((leaf_attr(c0) ? M_BX_R : M_BC_R) + bo, w[c0].y); --fp; }
+               else { emit((leaf_attr(c0) ? M_BR_R : M_BC_R) + bo, w[c0].y); --fp; }
             } else {
                const bool left_first = node_need(w[c0]) >= node_need(w[c1]);
                const int first = left_first ? c0 : c1, second = left_first ? c1 : c0;
@@ -166,13 +167,12 @@ __global__ void translate_kernel(const TranslateArgs a) {
                   frames[fp - 1] = frame(node, d, 1);
                   frames[fp++] = frame(first, d, 0);
                } else if (st == 1) {
-                  emit(M_PUSH + (uint32_t)d, 0u);
+                  emit(M_PUSH, slot0 + (uint32_t)d);
                   frames[fp - 1] = frame(node, d, 2);
                   frames[fp++] = frame(second, d + 1, 0);
                } else {
-                  emit(M_FETCHB + (uint32_t)d, 0u);
-                  // slot holds `first`; acc holds `second`
-                  emit((left_first ? M_BB_R : M_BB_L) + bo, 0u);
+                  // slot d holds `first`, acc holds `second`
+                  emit((left_first ? M_BR_R : M_BR_L) + bo, slot0 + (uint32_t)d);
                   --fp;
                }
             }
@@ -189,23 +189,21 @@ __global__ void translate_kernel(const TranslateArgs a) {
             frames[fp - 1] = frame(node, d, 1);
             frames[fp++] = frame(x[0], d, 0);
          } else if (st == 1) {
-            emit(M_PUSH + (uint32_t)d, 0u);
+            emit(M_PUSH, slot0 + (uint32_t)d);
             frames[fp - 1] = frame(node, d, 2);
             frames[fp++] = frame(x[1], d + 1, 0);
          } else if (st == 2) {
-            emit(M_PUSH + (uint32_t)(d + 1), 0u);
+            emit(M_PUSH, slot0 + (uint32_t)(d + 1));
             frames[fp - 1] = frame(node, d, 3);
             frames[fp++] = frame(x[2], d + 2, 0);
          } else {
-            emit(M_FETCHB + (uint32_t)d, 0u);
-            emit(M_FETCHC + (uint32_t)(d + 1), 0u);
-            // x[0] -> b (1), x[1] -> c (2), x[2] -> acc (0)
+            // x[0] -> row a (1), x[1] -> row b (2), x[2] -> acc (0)
             auto reg = [&](int child) { return child == x[0] ? 1 : (child == x[1] ? 2 : 0); };
             const int rc = reg(c0), rt = reg(c1), re = reg(c2);
             int perm = 0;
             for (int p = 0; p < 6; ++p)
                if (ite_role(p, 0) == rc && ite_role(p, 1) == rt && ite_role(p, 2) == re) perm = p;
-            emit(M_ITE + (uint32_t)perm, 0u);
+            emit(M_ITE + (uint32_t)perm, (slot0 + (uint32_t)d) | ((slot0 + (uint32_t)d + 1) << 16));
             --fp;
          }
       }

@@ -86,6 +86,7 @@ def load_library():
     L.ppi_gpu_last_kernel_ms.argtypes = [C.c_void_p, _fp]
     L.ppi_gpu_last_launch_count.argtypes = [C.c_void_p]
     L.ppi_gpu_last_stage_ms.argtypes = [C.c_void_p, _fp, _fp]
+    L.ppi_gpu_lanes.argtypes = [C.c_void_p]
     _lib = L
     return L
 
@@ -222,6 +223,10 @@ class Evaluator:
         t = np.zeros(2, np.float32)
         self._check(self._L.ppi_gpu_last_stage_ms(self._h, _f(t[0:1]), _f(t[1:2])))
         return float(t[0]), float(t[1])
+
+    @property
+    def lanes(self):
+        return int(self._L.ppi_gpu_lanes(self._h))
 
     def last_launch_count(self):
         return int(self._L.ppi_gpu_last_launch_count(self._h))

@@ -34,7 +34,7 @@ def test_strategy_orders_bitexact(gpu_lib, oracle_lib, name, strat, lanes):
     d = load_golden(name)
     ev = make_evaluator(d, strat, lanes, "parity")
     f, best = ev.evaluate(d["phenotype"], d["ephemeral"], d["size"], float(d["alpha"]))
-    L = lanes if lanes > 0 else min(len(d["rows"]), 1024)
+    L = ev.lanes
     ref = oracle_for(oracle_lib, d).evaluate(d["phenotype"], d["ephemeral"], d["size"], strat, L,
                                             float(d["alpha"]))
     assert_bitexact(f, ref, "%s %s%d" % (name, strat, lanes))

@@ -20,7 +20,10 @@ def _dataset(rng, nlin, nfeat, ef="abs"):
 def _check(oracle_lib, d, rows, ph, ep, sz, strat, lanes, math="parity", alpha=1e-6):
     ev = make_evaluator(d, strat, lanes, math, population=len(sz), max_size=ph.shape[1], rows=rows)
     f, best = ev.evaluate(ph, ep, sz, alpha)
-    L = 1 if strat == "PP" else (lanes if lanes > 0 else min(len(rows), 1024))
+    L = ev.lanes
+    assert L == (1 if strat == "PP" else lanes if lanes > 0 and strat == "DP" else
+                 min(lanes, len(rows)) if lanes > 0 else
+                 min(len(rows), 1024) if strat == "PDP" else min(1024, -(-len(rows) // 152)))
     ref = oracle_for(oracle_lib, d, rows=rows).evaluate(ph, ep, sz, strat, L, alpha)
     assert_bitexact(f, ref, "%s%d" % (strat, lanes))
     assert best == oracle_lib.best_index(ref)
