@@ -202,6 +202,31 @@ int32_t ppi_gpu_lanes(const ppi_gpu* h);
 /* Number of kernel launches the last evaluate / predict / decode call made. */
 int32_t ppi_gpu_last_launch_count(const ppi_gpu* h);
 
+/* No counterpart in the reference.  One generation evaluated without
+ * allocating any memory, for callers that cannot allocate where they evaluate:
+ * an application whose device memory another allocator has already reserved,
+ * an island process that must keep a fixed footprint once running, or a loop
+ * that cannot afford the device-wide synchronisation of cudaMalloc/cudaFree.
+ * The caller passes everything in device memory it owns: the dataset
+ * column-major (column c at d_data + c*ld, ld >= nlin, ld a multiple of 4,
+ * d_data 16-byte aligned, target in the last column), the programs (rows of
+ * config->max_size) and the outputs.  Work is queued on `stream` (a
+ * cudaStream_t); the call does not synchronise.  config->population_size is
+ * ignored; config->symbols and config->cost are read during the call.
+ * Scratch comes from one fixed 64 MiB array inside the library, which every
+ * GPU that loads the library holds until exit.  A batch needing more
+ * (about 16,000 programs of max_size 128) is rejected with
+ * PPI_ERR_UNSUPPORTED and a message on stderr.  The first call on each device
+ * looks up the array's device address, so make it before any stream capture.
+ * All calls share the array: calls that overlap on the GPU race, so
+ * serialise them.  Programs the generic interpreter cannot hold get FLT_MAX
+ * here without a status report. */
+ppi_status ppi_gpu_evaluate_noalloc(const ppi_gpu_config* config, const float* d_data,
+                                    int32_t nlin, int32_t ncol, int32_t ld,
+                                    const int32_t* d_phenotype, const float* d_ephemeral,
+                                    const int32_t* d_size, int32_t n, float alpha,
+                                    float* d_fitness, int32_t* d_best_index, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -123,6 +123,7 @@ class Evaluator:
                      _f(self._cost) if self._cost is not None else None,
                      0 if self._cost is None else self._cost.shape[0], self._syms, len(sv),
                      device)
+        self._config = cfg
         h = C.c_void_p()
         st = L.ppi_gpu_create(C.byref(cfg), C.byref(h))
         if st != 0:
