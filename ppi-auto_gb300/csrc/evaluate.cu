@@ -1,501 +1,105 @@
-// evaluate.cu -- fitness of every program over every record, on sm_103a.
-//
-// Execution model (GB300-first):
-//   * one CTA of P threads evaluates one program at a time, pulling program
-//     indices from a device work queue (persistent grid, one wave of CTAs);
-//   * the dataset is column-major in HBM; each CTA stages a tile of
-//     T = P * kR records (all columns) into shared memory with 16-byte
-//     vector loads, so attribute reads are conflict-free LDS.128;
-//   * the program's bytecode sits in shared memory and every warp walks it in
-//     lock step: instruction dispatch is warp-uniform (no divergence) and each
-//     instruction is applied to the kR records a thread holds in registers
-//     (acc / b / c / kSlots slots), giving kR-way ILP;
-//   * errors are reduced in exactly the order of the reference strategy:
-//       PDP (lanes == T): lane = tile position, accumulated in registers;
-//       PDP (other lanes) and PP (lanes == 1): per-lane accumulators in
-//         shared memory, each lane adding its records in increasing order;
-//       DP: per-group trees in shared memory, groups added in order;
-//     then the reference's local tree (accelerator.cl:157-167, 252-262);
-//   * fitness, alpha*size and the arg-min (64-bit packed atomicMin) are fused
-//     into the same kernel; the last CTA to finish writes the best index.
+// evaluate.cu -- launch geometry and math-mode dispatch of the evaluator
+// kernels (evaluate_impl.cuh, instantiated in evaluate_{fast,parity,native}.cu).
+#include <algorithm>
+#include <cmath>
+#include <cstdlib>
+
 #include "ppi_internal.cuh"
 
 namespace ppi {
-namespace {
 
-constexpr uint32_t kGenericEnd = 0xFFFFu;
+cudaError_t launch_evaluate_fast(int R, const EvalArgs& a, int block, int grid, size_t smem, cudaStream_t s);
+cudaError_t launch_evaluate_parity(int R, const EvalArgs& a, int block, int grid, size_t smem, cudaStream_t s);
+cudaError_t launch_evaluate_native(int R, const EvalArgs& a, int block, int grid, size_t smem, cudaStream_t s);
+cudaError_t launch_predict_fast(int R, const PredictArgs& a, int block, int grid, size_t smem, cudaStream_t s);
+cudaError_t launch_predict_parity(int R, const PredictArgs& a, int block, int grid, size_t smem, cudaStream_t s);
+cudaError_t launch_predict_native(int R, const PredictArgs& a, int block, int grid, size_t smem, cudaStream_t s);
+cudaError_t evaluate_occupancy_fast(int R, int block, size_t smem, int* per_sm);
+cudaError_t evaluate_occupancy_parity(int R, int block, size_t smem, int* per_sm);
+cudaError_t evaluate_occupancy_native(int R, int block, size_t smem, int* per_sm);
 
-__device__ __forceinline__ size_t code_bytes(int code_stride) {
-   return ((size_t)(code_stride + 1) * sizeof(uint2) + 15) & ~(size_t)15;
-}
-
-__device__ __forceinline__ void load_row(const float* p, float (&x)[kR]) {
-   const float4* q = reinterpret_cast<const float4*>(p);
-   const float4 u = q[0], v = q[1];
-   x[0] = u.x; x[1] = u.y; x[2] = u.z; x[3] = u.w;
-   x[4] = v.x; x[5] = v.y; x[6] = v.z; x[7] = v.w;
-}
-__device__ __forceinline__ void store_row(float* p, const float (&x)[kR]) {
-   float4* q = reinterpret_cast<float4*>(p);
-   q[0] = make_float4(x[0], x[1], x[2], x[3]);
-   q[1] = make_float4(x[4], x[5], x[6], x[7]);
-}
-static_assert(kR == 8, "load_row assumes 8 records per thread");
-
-// ---- bytecode path -------------------------------------------------------------
-// `mine` points at this thread's kR positions of row 0; row k is at mine + k*T.
-template <int MATH>
-__device__ __forceinline__ void run_fast(const uint2* __restrict__ code, float* mine, int T,
-                                         float (&acc)[kR], int prot) {
-   int pc = 0;
-   uint2 ins = code[0];
-   for (;;) {
-      const uint2 nxt = code[pc + 1];
-      switch (ins.x) {
-      case M_END: return;
-      case M_LD_ROW: load_row(mine + (size_t)ins.y * T, acc); break;
-      case M_LD_C: {
-         const float k = __uint_as_float(ins.y);
-#pragma unroll
-         for (int r = 0; r < kR; ++r) acc[r] = k;
-         break;
-      }
-      case M_PUSH: store_row(mine + (size_t)ins.y * T, acc); break;
-
-#define PPI_UN_CASE(OP)                                                            \
-      case M_UN + (OP - PPI_OP_NOT):                                               \
-         _Pragma("unroll") for (int r = 0; r < kR; ++r) acc[r] = unop<OP, MATH>(acc[r], prot); \
-         break;
-      PPI_UN_CASE(PPI_OP_NOT) PPI_UN_CASE(PPI_OP_ABS) PPI_UN_CASE(PPI_OP_POW2)
-      PPI_UN_CASE(PPI_OP_POW3) PPI_UN_CASE(PPI_OP_POW4) PPI_UN_CASE(PPI_OP_POW5)
-      PPI_UN_CASE(PPI_OP_NEG) PPI_UN_CASE(PPI_OP_ROUND) PPI_UN_CASE(PPI_OP_CEIL)
-      PPI_UN_CASE(PPI_OP_FLOOR) PPI_UN_CASE(PPI_OP_EXP) PPI_UN_CASE(PPI_OP_EXP10)
-      PPI_UN_CASE(PPI_OP_EXP2) PPI_UN_CASE(PPI_OP_SIN) PPI_UN_CASE(PPI_OP_COS)
-      PPI_UN_CASE(PPI_OP_STEP) PPI_UN_CASE(PPI_OP_SIGN) PPI_UN_CASE(PPI_OP_LOGISTIC)
-      PPI_UN_CASE(PPI_OP_GAMMA) PPI_UN_CASE(PPI_OP_GAUSS) PPI_UN_CASE(PPI_OP_SQRT)
-      PPI_UN_CASE(PPI_OP_LOG) PPI_UN_CASE(PPI_OP_LOG10) PPI_UN_CASE(PPI_OP_LOG2)
-      PPI_UN_CASE(PPI_OP_TAN)
-#undef PPI_UN_CASE
-
-#define PPI_BIN_CASES(OP)                                                          \
-      case M_BR_L + (OP - PPI_OP_AND): {                                           \
-         float x[kR];                                                              \
-         load_row(mine + (size_t)ins.y * T, x);                                    \
-         _Pragma("unroll") for (int r = 0; r < kR; ++r) acc[r] = binop<OP, MATH>(acc[r], x[r], prot); \
-         break;                                                                    \
-      }                                                                            \
-      case M_BR_R + (OP - PPI_OP_AND): {                                           \
-         float x[kR];                                                              \
-         load_row(mine + (size_t)ins.y * T, x);                                    \
-         _Pragma("unroll") for (int r = 0; r < kR; ++r) acc[r] = binop<OP, MATH>(x[r], acc[r], prot); \
-         break;                                                                    \
-      }                                                                            \
-      case M_BC_L + (OP - PPI_OP_AND): {                                           \
-         const float k = __uint_as_float(ins.y);                                   \
-         _Pragma("unroll") for (int r = 0; r < kR; ++r) acc[r] = binop<OP, MATH>(acc[r], k, prot); \
-         break;                                                                    \
-      }                                                                            \
-      case M_BC_R + (OP - PPI_OP_AND): {                                           \
-         const float k = __uint_as_float(ins.y);                                   \
-         _Pragma("unroll") for (int r = 0; r < kR; ++r) acc[r] = binop<OP, MATH>(k, acc[r], prot); \
-         break;                                                                    \
-      }
-      PPI_BIN_CASES(PPI_OP_AND) PPI_BIN_CASES(PPI_OP_OR) PPI_BIN_CASES(PPI_OP_XOR)
-      PPI_BIN_CASES(PPI_OP_GREATER) PPI_BIN_CASES(PPI_OP_GREATEREQUAL)
-      PPI_BIN_CASES(PPI_OP_LESS) PPI_BIN_CASES(PPI_OP_LESSEQUAL) PPI_BIN_CASES(PPI_OP_EQUAL)
-      PPI_BIN_CASES(PPI_OP_NOTEQUAL) PPI_BIN_CASES(PPI_OP_ADD) PPI_BIN_CASES(PPI_OP_SUB)
-      PPI_BIN_CASES(PPI_OP_MULT) PPI_BIN_CASES(PPI_OP_MEAN) PPI_BIN_CASES(PPI_OP_MAX)
-      PPI_BIN_CASES(PPI_OP_MIN) PPI_BIN_CASES(PPI_OP_MOD) PPI_BIN_CASES(PPI_OP_POW)
-      PPI_BIN_CASES(PPI_OP_DIV)
-#undef PPI_BIN_CASES
-
-#define PPI_ITE_CASE(P)                                                            \
-      case M_ITE + P: {                                                            \
-         float ra[kR], rb[kR];                                                     \
-         load_row(mine + (size_t)(ins.y & 0xFFFFu) * T, ra);                       \
-         load_row(mine + (size_t)(ins.y >> 16) * T, rb);                           \
-         _Pragma("unroll") for (int r = 0; r < kR; ++r) {                          \
-            const float v3[3] = {acc[r], ra[r], rb[r]};                            \
-            acc[r] = truthy(v3[ite_role(P, 0)]) ? v3[ite_role(P, 1)] : v3[ite_role(P, 2)]; \
-         }                                                                         \
-         break;                                                                    \
-      }
-      PPI_ITE_CASE(0) PPI_ITE_CASE(1) PPI_ITE_CASE(2) PPI_ITE_CASE(3) PPI_ITE_CASE(4)
-      PPI_ITE_CASE(5)
-#undef PPI_ITE_CASE
-      default: __builtin_unreachable();
-      }
-      ins = nxt;
-      ++pc;
-   }
-}
-
-// ---- generic stack interpreter ----------------------------------------------
-template <int MATH>
-__device__ __forceinline__ float generic_op(int op, float a, float b, int prot) {
-   switch (op) {
-#define PPI_GU(OP) case OP: return unop<OP, MATH>(a, prot);
-      PPI_GU(PPI_OP_NOT) PPI_GU(PPI_OP_ABS) PPI_GU(PPI_OP_POW2) PPI_GU(PPI_OP_POW3)
-      PPI_GU(PPI_OP_POW4) PPI_GU(PPI_OP_POW5) PPI_GU(PPI_OP_NEG) PPI_GU(PPI_OP_ROUND)
-      PPI_GU(PPI_OP_CEIL) PPI_GU(PPI_OP_FLOOR) PPI_GU(PPI_OP_EXP) PPI_GU(PPI_OP_EXP10)
-      PPI_GU(PPI_OP_EXP2) PPI_GU(PPI_OP_SIN) PPI_GU(PPI_OP_COS) PPI_GU(PPI_OP_STEP)
-      PPI_GU(PPI_OP_SIGN) PPI_GU(PPI_OP_LOGISTIC) PPI_GU(PPI_OP_GAMMA) PPI_GU(PPI_OP_GAUSS)
-      PPI_GU(PPI_OP_SQRT) PPI_GU(PPI_OP_LOG) PPI_GU(PPI_OP_LOG10) PPI_GU(PPI_OP_LOG2)
-      PPI_GU(PPI_OP_TAN)
-#undef PPI_GU
-#define PPI_GB(OP) case OP: return binop<OP, MATH>(a, b, prot);
-      PPI_GB(PPI_OP_AND) PPI_GB(PPI_OP_OR) PPI_GB(PPI_OP_XOR) PPI_GB(PPI_OP_GREATER)
-      PPI_GB(PPI_OP_GREATEREQUAL) PPI_GB(PPI_OP_LESS) PPI_GB(PPI_OP_LESSEQUAL)
-      PPI_GB(PPI_OP_EQUAL) PPI_GB(PPI_OP_NOTEQUAL) PPI_GB(PPI_OP_ADD) PPI_GB(PPI_OP_SUB)
-      PPI_GB(PPI_OP_MULT) PPI_GB(PPI_OP_MEAN) PPI_GB(PPI_OP_MAX) PPI_GB(PPI_OP_MIN)
-      PPI_GB(PPI_OP_MOD) PPI_GB(PPI_OP_POW) PPI_GB(PPI_OP_DIV)
-#undef PPI_GB
-   default: return __uint_as_float(0x7fc00000u);
-   }
-}
-
-// Right-to-left stack evaluation with the reference's stack semantics
-// (accelerator.cl:28-53); missing operands of a malformed program read as NaN.
-template <int MATH>
-__device__ __noinline__ void run_generic(const uint2* __restrict__ code, const float* __restrict__ tile,
-                                         int T, int tid, float* __restrict__ out, int prot) {
-   float stk[kGenericStack];
-   const float qnan = __uint_as_float(0x7fc00000u);
-#pragma unroll 1
-   for (int r = 0; r < kR; ++r) {
-      int top = -1;
-      const int rec = tid * kR + r;
-#pragma unroll 1
-      for (int pc = 0;; ++pc) {
-         const uint2 ins = code[pc];
-         const int op = (int)ins.x;
-         if (ins.x == kGenericEnd) break;
-         const int ar = op_arity(op);
-         if (top + 1 < ar) {
-            const int have = top + 1, miss = ar - have;
-            for (int k = have - 1; k >= 0; --k) stk[k + miss] = stk[k];
-            for (int k = 0; k < miss; ++k) stk[k] = qnan;
-            top = ar - 1;
-         }
-         if (ar == 0) {
-            float v;
-            if (op == PPI_OP_ATTRIBUTE) v = tile[(size_t)ins.y * T + rec];
-            else v = __uint_as_float(ins.y);   // CONST / LITERAL value, INVALID = NaN
-            stk[++top] = v;
-         } else if (ar == 3) {
-            stk[top - 2] = truthy(stk[top]) ? stk[top - 1] : stk[top - 2];
-            top -= 2;
-         } else if (ar == 2) {
-            stk[top - 1] = generic_op<MATH>(op, stk[top], stk[top - 1], prot);
-            --top;
-         } else {
-            stk[top] = generic_op<MATH>(op, stk[top], 0.0f, prot);
-         }
-      }
-      out[r] = top >= 0 ? stk[top] : qnan;
-   }
-}
-
-__device__ __forceinline__ void stage_tile(const EvalArgs& a, float* s_tile, int base, int T,
-                                           int tid, int P) {
-   const bool vec = (base & 3) == 0;
-   for (int cidx = 0; cidx < a.ncol; ++cidx) {
-      const float* src = a.data + (size_t)cidx * a.ld + base;
-      float* dst = s_tile + (size_t)cidx * T;
-      for (int t = tid * 4; t < T; t += P * 4) {
-         if (vec && base + t + 3 < a.ld) {
-            *reinterpret_cast<float4*>(dst + t) = __ldg(reinterpret_cast<const float4*>(src + t));
-         } else {
-#pragma unroll
-            for (int j = 0; j < 4; ++j) dst[t + j] = (base + t + j < a.ld) ? __ldg(src + t + j) : 0.0f;
-         }
-      }
-   }
-}
-
-__device__ __forceinline__ unsigned long long fitness_key(float f, int prog) {
-   uint32_t u = __float_as_uint(f);
-   u = (u & 0x80000000u) ? ~u : (u | 0x80000000u);
-   return ((unsigned long long)u << 32) | (unsigned long long)(0xFFFFFFFFu - (uint32_t)prog);
-}
-
-__device__ __forceinline__ float reduce1(int reduce_max, float acc, float e, float fnlin) {
-   if (reduce_max) {
-      const float v = e * fnlin;
-      return (v > acc) ? v : acc;
-   }
-   return acc + e;
-}
-
-// __local tree of accelerator.cl:157-167 / 252-262 over L values.
-__device__ __forceinline__ void local_tree(float* pe, int L, int reduce_max, int tid, int P) {
-   int p2 = 1;
-   while (p2 < L) p2 <<= 1;
-   for (int s = p2 >> 1; s > 0; s >>= 1) {
-      for (int l = tid; l < s; l += P)
-         if (l + s < L) pe[l] = reduce_max ? ((pe[l + s] > pe[l]) ? pe[l + s] : pe[l]) : pe[l] + pe[l + s];
-      __syncthreads();
-   }
-}
-
-template <int MATH>
-__global__ void __launch_bounds__(128, 4) eval_kernel(const EvalArgs a) {
-   extern __shared__ __align__(16) unsigned char smem_raw[];
-   __shared__ int s_prog;
-   const int P = blockDim.x, tid = threadIdx.x, T = P * kR;
-   const int L = a.lanes;
-   uint2* s_code = reinterpret_cast<uint2*>(smem_raw);
-   float* s_tile = reinterpret_cast<float*>(smem_raw + code_bytes(a.code_stride));
-   float* s_err = s_tile + (size_t)(a.ncol + kSlots) * T;
-   float* s_acc = s_err + T;
-   int* s_done = reinterpret_cast<int*>(s_acc + L);
-   const bool aligned = a.strategy == PPI_STRATEGY_PDP && L == T;
-   const bool dp = a.strategy == PPI_STRATEGY_DP;
-   const int Teff = dp ? L * (T / L) : T;
-   const float fnlin = (float)a.nlin;
-
-   for (;;) {
-      if (tid == 0) s_prog = (int)atomicAdd(&a.counters[0], 1u);
-      __syncthreads();
-      const int prog = s_prog;
-      if (prog >= a.n) break;
-      const int2 m = a.meta[prog];
-      const int size = a.size[prog];
-      float fit = FLT_MAX;
-      if (m.x == kKindInvalid || m.x == kKindUnsupported) {
-         // size 0 (sizes outside [1, max_size] are treated as 0)
-         if (tid == 0) {
-            if (m.x == kKindUnsupported) atomicOr(a.status, kStatusUnsupportedProgram);
-            if (m.x == kKindInvalid && dp) {
-               // every group reports MAXFLOAT (accelerator.cl:108-112); host rule
-               float sum = 0.0f;
-               const int G = (a.nlin + L - 1) / L;
-               for (int g = 0; g < G; ++g) sum = reduce1(a.reduce_max, sum, FLT_MAX, fnlin);
-               fit = nonfinite(sum) ? FLT_MAX : sum / fnlin;
-            }
-         }
-      } else {
-         const uint2* g = a.code + (size_t)prog * a.code_stride;
-         for (int i = tid; i < m.y; i += P) s_code[i] = g[i];
-         if (!aligned)
-            for (int l = tid; l < L; l += P) { s_acc[l] = 0.0f; s_done[l] = 0; }
-         float lacc[kR];
-#pragma unroll
-         for (int r = 0; r < kR; ++r) lacc[r] = 0.0f;
-         uint32_t ldone = 0u;
-         float dsum = 0.0f;
-         bool ddone = false;
-         for (int base = 0; base < a.nlin; base += Teff) {
-            __syncthreads();
-            stage_tile(a, s_tile, base, T, tid, P);
-            __syncthreads();
-            float v[kR];
-            if (m.x == kKindFast) {
-               run_fast<MATH>(s_code, s_tile + tid * kR, T, v, a.prot);
-            } else {
-               float tmp[kR];
-               run_generic<MATH>(s_code, s_tile, T, tid, tmp, a.prot);
-#pragma unroll
-               for (int r = 0; r < kR; ++r) v[r] = tmp[r];
-            }
-            const float* ycol = s_tile + (size_t)(a.ncol - 1) * T + tid * kR;
-            float e[kR];
-#pragma unroll
-            for (int r = 0; r < kR; ++r) e[r] = apply_error(a.ef, v[r], ycol[r], a.cost, a.cost_n);
-            if (aligned) {
-#pragma unroll
-               for (int r = 0; r < kR; ++r) {
-                  const int n = base + tid * kR + r;
-                  if (n < a.nlin && !((ldone >> r) & 1u)) {
-                     if (nonfinite(e[r])) { lacc[r] = FLT_MAX; ldone |= 1u << r; }
-                     else lacc[r] = reduce1(a.reduce_max, lacc[r], e[r], fnlin);
-                  }
-               }
-            } else {
-#pragma unroll
-               for (int r = 0; r < kR; ++r) {
-                  const int t = tid * kR + r;
-                  s_err[t] = (dp && base + t >= a.nlin) ? 0.0f : e[r];
-               }
-               __syncthreads();
-               if (dp) {
-                  const int G = Teff / L;
-                  int p2 = 1;
-                  while (p2 < L) p2 <<= 1;
-                  for (int s = p2 >> 1; s > 0; s >>= 1) {
-                     for (int idx = tid; idx < G * s; idx += P) {
-                        const int gi = idx / s, l = idx - gi * s;
-                        if (l + s < L) {
-                           float* pe = s_err + gi * L;
-                           pe[l] = a.reduce_max ? ((pe[l + s] > pe[l]) ? pe[l + s] : pe[l]) : pe[l] + pe[l + s];
-                        }
-                     }
-                     __syncthreads();
-                  }
-                  if (tid == 0) {
-                     for (int gi = 0; gi < G && !ddone; ++gi) {
-                        if (base + gi * L >= a.nlin) break;
-                        const float part = s_err[gi * L];
-                        if (nonfinite(part)) { dsum = FLT_MAX; ddone = true; }
-                        else dsum = reduce1(a.reduce_max, dsum, part, fnlin);
-                     }
-                  }
-               } else {
-                  const int end = min(base + T, a.nlin);
-                  const int off = base % L;
-                  for (int l = tid; l < L; l += P) {
-                     if (s_done[l]) continue;
-                     float acc = s_acc[l];
-                     int done = 0;
-                     for (int n = base + (l - off + L) % L; n < end; n += L) {
-                        const float ev = s_err[n - base];
-                        if (nonfinite(ev)) { acc = FLT_MAX; done = 1; break; }
-                        acc = reduce1(a.reduce_max, acc, ev, fnlin);
-                     }
-                     s_acc[l] = acc;
-                     if (done) s_done[l] = 1;
-                  }
-               }
-            }
-         }
-         __syncthreads();
-         if (dp) {
-            if (tid == 0) fit = nonfinite(dsum) ? FLT_MAX : dsum / fnlin + a.alpha * (float)size;
-         } else {
-            if (aligned) {
-#pragma unroll
-               for (int r = 0; r < kR; ++r) s_acc[tid * kR + r] = lacc[r];
-               __syncthreads();
-            }
-            local_tree(s_acc, L, a.reduce_max, tid, P);
-            if (tid == 0) {
-               const float pe = s_acc[0];
-               const float vv = nonfinite(pe) ? FLT_MAX : pe / fnlin;
-               fit = vv + a.alpha * (float)size;
-            }
-         }
-      }
-      if (tid == 0) {
-         a.fitness[prog] = fit;
-         atomicMin(a.best_key, fitness_key(fit, prog));
-      }
-      __syncthreads();
-   }
-   if (tid == 0) {
-      __threadfence();
-      const unsigned done = atomicAdd(&a.counters[1], 1u);
-      if (done == gridDim.x - 1) {
-         __threadfence();
-         const unsigned long long k = *reinterpret_cast<volatile unsigned long long*>(a.best_key);
-         a.best_index[0] = (int32_t)(0xFFFFFFFFu - (uint32_t)(k & 0xFFFFFFFFull));
-      }
-   }
-}
-
-// Per-record predictions of program 0 (ppp prediction mode).
-template <int MATH>
-__global__ void __launch_bounds__(128, 4) predict_kernel(const PredictArgs a) {
-   extern __shared__ __align__(16) unsigned char smem_raw[];
-   const int P = blockDim.x, tid = threadIdx.x, T = P * kR;
-   const int2 m = a.meta[0];
-   uint2* s_code = reinterpret_cast<uint2*>(smem_raw);
-   float* s_tile = reinterpret_cast<float*>(smem_raw + code_bytes(m.y));
-   for (int i = tid; i < m.y; i += P) s_code[i] = a.code[i];
-   EvalArgs ea{};
-   ea.data = a.data;
-   ea.nlin = a.nlin;
-   ea.ncol = a.ncol;
-   ea.ld = a.ld;
-   for (int base = blockIdx.x * T; base < a.nlin; base += gridDim.x * T) {
-      __syncthreads();
-      stage_tile(ea, s_tile, base, T, tid, P);
-      __syncthreads();
-      float v[kR];
-      if (m.x == kKindFast) {
-         run_fast<MATH>(s_code, s_tile + tid * kR, T, v, a.prot);
-      } else if (m.x == kKindGeneric) {
-         float tmp[kR];
-         run_generic<MATH>(s_code, s_tile, T, tid, tmp, a.prot);
-#pragma unroll
-         for (int r = 0; r < kR; ++r) v[r] = tmp[r];
-      } else {
-#pragma unroll
-         for (int r = 0; r < kR; ++r) v[r] = __uint_as_float(0x7fc00000u);
-      }
-#pragma unroll
-      for (int r = 0; r < kR; ++r) {
-         const int n = base + tid * kR + r;
-         if (n < a.nlin) a.out[n] = v[r];
-      }
-   }
-}
-
-template <int MATH>
-cudaError_t launch_eval_t(const EvalArgs& a, int block, int grid, size_t smem, cudaStream_t s) {
-   static bool configured = false;
-   if (!configured) {
-      cudaError_t e = cudaFuncSetAttribute(eval_kernel<MATH>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-      if (e != cudaSuccess) return e;
-      configured = true;
-   }
-   eval_kernel<MATH><<<grid, block, smem, s>>>(a);
-   return cudaGetLastError();
-}
-
-template <int MATH>
-cudaError_t launch_predict_t(const PredictArgs& a, int block, int grid, size_t smem, cudaStream_t s) {
-   static bool configured = false;
-   if (!configured) {
-      cudaError_t e = cudaFuncSetAttribute(predict_kernel<MATH>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-      if (e != cudaSuccess) return e;
-      configured = true;
-   }
-   predict_kernel<MATH><<<grid, block, smem, s>>>(a);
-   return cudaGetLastError();
-}
-
-}  // namespace
-
-size_t evaluate_smem_bytes(int code_stride, int ncol, int block, int lanes) {
-   const size_t T = (size_t)block * kR;
+size_t evaluate_smem_bytes(int code_stride, int ncol, int block, int R, int lanes, bool aligned) {
+   const size_t T = (size_t)block * R;
    const size_t code = ((size_t)(code_stride + 1) * sizeof(uint2) + 15) & ~(size_t)15;
-   return code + (size_t)(ncol + kSlots) * T * 4 + T * 4 + (size_t)lanes * 8;
+   const size_t rows = (size_t)(ncol + kSlots) * T * 4;
+   if (aligned) return code + std::max(rows, (size_t)lanes * 4);
+   return code + rows + T * 4 + (size_t)lanes * 8;
 }
 
-cudaError_t launch_evaluate(int math, const EvalArgs& a, int block, int grid, size_t smem,
+cudaError_t launch_evaluate(int math, int R, const EvalArgs& a, int block, int grid, size_t smem,
                             cudaStream_t s) {
    switch (math) {
-   case kMathParity: return launch_eval_t<kMathParity>(a, block, grid, smem, s);
-   case kMathNative: return launch_eval_t<kMathNative>(a, block, grid, smem, s);
-   default: return launch_eval_t<kMathFast>(a, block, grid, smem, s);
+   case kMathParity: return launch_evaluate_parity(R, a, block, grid, smem, s);
+   case kMathNative: return launch_evaluate_native(R, a, block, grid, smem, s);
+   default: return launch_evaluate_fast(R, a, block, grid, smem, s);
    }
 }
 
-cudaError_t launch_predict(int math, const PredictArgs& a, int block, int grid, size_t smem,
+cudaError_t launch_predict(int math, int R, const PredictArgs& a, int block, int grid, size_t smem,
                            cudaStream_t s) {
    switch (math) {
-   case kMathParity: return launch_predict_t<kMathParity>(a, block, grid, smem, s);
-   case kMathNative: return launch_predict_t<kMathNative>(a, block, grid, smem, s);
-   default: return launch_predict_t<kMathFast>(a, block, grid, smem, s);
+   case kMathParity: return launch_predict_parity(R, a, block, grid, smem, s);
+   case kMathNative: return launch_predict_native(R, a, block, grid, smem, s);
+   default: return launch_predict_fast(R, a, block, grid, smem, s);
    }
 }
 
-cudaError_t evaluate_occupancy(int math, int block, size_t smem, int* blocks_per_sm) {
-   cudaError_t e;
+cudaError_t evaluate_occupancy(int math, int R, int block, size_t smem, int* per_sm) {
    switch (math) {
-   case kMathParity:
-      e = cudaFuncSetAttribute(eval_kernel<kMathParity>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-      if (e != cudaSuccess) return e;
-      return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, eval_kernel<kMathParity>, block, smem);
-   case kMathNative:
-      e = cudaFuncSetAttribute(eval_kernel<kMathNative>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-      if (e != cudaSuccess) return e;
-      return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, eval_kernel<kMathNative>, block, smem);
-   default:
-      e = cudaFuncSetAttribute(eval_kernel<kMathFast>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-      if (e != cudaSuccess) return e;
-      return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, eval_kernel<kMathFast>, block, smem);
+   case kMathParity: return evaluate_occupancy_parity(R, block, smem, per_sm);
+   case kMathNative: return evaluate_occupancy_native(R, block, smem, per_sm);
+   default: return evaluate_occupancy_fast(R, block, smem, per_sm);
    }
+}
+
+int resolve_lanes(int strategy, int lanes, int nlin, int sm_count) {
+   // -cl-mls when given; else the reference's rule (accelerator.cc:296-330) on
+   // a device with 1024-wide work-groups and sm_count compute units.
+   if (strategy == PPI_STRATEGY_PP) return 1;
+   if (lanes <= 0 && strategy == PPI_STRATEGY_PDP) return std::min(nlin, 1024);
+   if (lanes <= 0) return std::min(1024, (int)std::ceil(nlin / (float)std::max(1, sm_count)));
+   if (strategy == PPI_STRATEGY_PDP) return std::min(lanes, nlin);
+   return lanes;
+}
+
+const char* plan_geometry(int strategy, int lanes, int math, int nlin, int ncol, int code_stride,
+                          int n_max, int sm_count, Geometry* g) {
+   const int L = lanes;
+   if (L < 1 || L > kMaxLanes) return "lane count out of range";
+   // records per thread: 8 (measured faster than 16 on GB300: more resident
+   // warps hide the dispatch latency); PPI_GPU_RECORDS_PER_THREAD=16 selects
+   // 16 where the lane == tile-position path allows it
+   const char* env = std::getenv("PPI_GPU_RECORDS_PER_THREAD");
+   const bool allow16 = env && std::atoi(env) == 16;
+   int R = 8, P;
+   if (strategy == PPI_STRATEGY_PDP && allow16 && L % (32 * 16) == 0 && L / 16 <= 128) {
+      R = 16;
+      P = L / 16;
+   } else if (strategy == PPI_STRATEGY_PDP && L % (32 * 8) == 0 && L / 8 <= 128) {
+      P = L / 8;
+   } else {
+      const int need = (strategy == PPI_STRATEGY_DP) ? L : std::min(nlin, 128 * 8);
+      P = std::min(128, std::max(32, ((need + 7) / 8 + 31) / 32 * 32));
+   }
+   if (strategy == PPI_STRATEGY_DP && L > P * R)
+      return "DP lanes above 1024 records per group are not supported";
+   bool aligned = strategy == PPI_STRATEGY_PDP && L == P * R;
+   size_t smem = evaluate_smem_bytes(code_stride, ncol, P, R, L, aligned);
+   while (smem > 200 * 1024 && P > 32 && !(strategy == PPI_STRATEGY_DP && L > (P / 2) * R)) {
+      P /= 2;
+      aligned = strategy == PPI_STRATEGY_PDP && L == P * R;
+      smem = evaluate_smem_bytes(code_stride, ncol, P, R, L, aligned);
+   }
+   if (smem > 200 * 1024) return "dataset has too many columns for one shared-memory tile";
+   int per_sm = 0;
+   if (evaluate_occupancy(math, R, P, smem, &per_sm) != cudaSuccess || per_sm < 1)
+      return "evaluator does not fit on an SM";
+   g->lanes = L;
+   g->block = P;
+   g->R = R;
+   g->smem = smem;
+   g->grid = std::max(1, std::min(n_max, per_sm * sm_count));
+   return nullptr;
 }
 
 }  // namespace ppi

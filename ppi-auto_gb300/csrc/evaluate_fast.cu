@@ -1,0 +1,16 @@
+// evaluate_fast.cu -- evaluator kernels instantiated for one math mode
+// (separate translation units so that the build compiles them in parallel).
+#include "evaluate_impl.cuh"
+
+namespace ppi {
+template struct ev::Launch<kMathFast>;
+cudaError_t launch_evaluate_fast(int R, const EvalArgs& a, int block, int grid, size_t smem, cudaStream_t s) {
+   return ev::Launch<kMathFast>::evaluate(R, a, block, grid, smem, s);
+}
+cudaError_t launch_predict_fast(int R, const PredictArgs& a, int block, int grid, size_t smem, cudaStream_t s) {
+   return ev::Launch<kMathFast>::predict(R, a, block, grid, smem, s);
+}
+cudaError_t evaluate_occupancy_fast(int R, int block, size_t smem, int* per_sm) {
+   return ev::Launch<kMathFast>::occupancy(R, block, smem, per_sm);
+}
+}  // namespace ppi

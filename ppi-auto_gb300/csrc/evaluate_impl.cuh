@@ -1,0 +1,483 @@
+// evaluate_impl.cuh -- fitness of every program over every record, on sm_103a.
+//
+// Execution model (GB300-first):
+//   * one CTA of P threads evaluates one program at a time, pulling program
+//     indices from a device work queue (persistent grid, one wave of CTAs);
+//   * the dataset is column-major in HBM; each CTA stages a tile of
+//     T = P * R records (all columns) into shared memory with 16-byte
+//     vector loads, so attribute reads are conflict-free LDS.128;
+//   * the program's bytecode sits in shared memory and every warp walks it in
+//     lock step: instruction dispatch is warp-uniform (no divergence) and each
+//     instruction is applied to the R records a thread holds in its
+//     accumulator registers (R-way ILP); operands other than the accumulator
+//     are shared-memory rows (data columns and slots);
+//   * errors are reduced in exactly the order of the reference strategy:
+//       PDP (lanes == T): lane = tile position, accumulated in registers;
+//       PDP (other lanes) and PP (lanes == 1): per-lane accumulators in
+//         shared memory, each lane adding its records in increasing order;
+//       DP: per-group trees in shared memory, groups added in order;
+//     then the reference's local tree (accelerator.cl:157-167, 252-262);
+//   * fitness, alpha*size and the arg-min (64-bit packed atomicMin) are fused
+//     into the same kernel; the last CTA to finish writes the best index.
+#pragma once
+
+#include "ppi_internal.cuh"
+
+namespace ppi {
+namespace ev {
+
+constexpr uint32_t kGenericEnd = 0xFFFFu;
+
+__device__ __forceinline__ size_t code_bytes(int code_stride) {
+   return ((size_t)(code_stride + 1) * sizeof(uint2) + 15) & ~(size_t)15;
+}
+
+// Tile layout: a thread's R records are R/4 quads of consecutive records;
+// quad i of thread tid starts at tile position (i*P + tid)*4, so the 16-byte
+// accesses of a warp cover 512 contiguous bytes (no bank conflicts for any R).
+__device__ __forceinline__ int tile_pos(int tid, int r, int P) { return ((r >> 2) * P + tid) * 4 + (r & 3); }
+
+// `p` points at this thread's first quad of a row; quads are 4*P floats apart.
+template <int R>
+__device__ __forceinline__ void load_row(const float* p, int P, float (&x)[R]) {
+   static_assert(R % 4 == 0, "rows are read as float4");
+#pragma unroll
+   for (int i = 0; i < R / 4; ++i) {
+      const float4 u = *reinterpret_cast<const float4*>(p + (size_t)i * 4 * P);
+      x[4 * i] = u.x; x[4 * i + 1] = u.y; x[4 * i + 2] = u.z; x[4 * i + 3] = u.w;
+   }
+}
+template <int R>
+__device__ __forceinline__ void store_row(float* p, int P, const float (&x)[R]) {
+#pragma unroll
+   for (int i = 0; i < R / 4; ++i)
+      *reinterpret_cast<float4*>(p + (size_t)i * 4 * P) = make_float4(x[4 * i], x[4 * i + 1], x[4 * i + 2], x[4 * i + 3]);
+}
+
+// ---- bytecode path -------------------------------------------------------------
+// `mine` points at this thread's first quad of row 0; row k is at mine + k*T.
+template <int MATH, int R>
+__device__ __forceinline__ void run_fast(const uint2* __restrict__ code, float* mine, int T, int P,
+                                         float (&acc)[R], int prot) {
+   int pc = 0;
+   uint2 ins = code[0];
+   for (;;) {
+      const uint2 nxt = code[pc + 1];
+      switch (ins.x) {
+      case M_END: return;
+      case M_LD_ROW: load_row(mine + (size_t)ins.y * T, P, acc); break;
+      case M_LD_C: {
+         const float k = __uint_as_float(ins.y);
+#pragma unroll
+         for (int r = 0; r < R; ++r) acc[r] = k;
+         break;
+      }
+      case M_PUSH: store_row(mine + (size_t)ins.y * T, P, acc); break;
+
+#define PPI_UN_CASE(OP)                                                            \
+      case M_UN + (OP - PPI_OP_NOT):                                               \
+         _Pragma("unroll") for (int r = 0; r < R; ++r) acc[r] = unop<OP, MATH>(acc[r], prot); \
+         break;
+      PPI_UN_CASE(PPI_OP_NOT) PPI_UN_CASE(PPI_OP_ABS) PPI_UN_CASE(PPI_OP_POW2)
+      PPI_UN_CASE(PPI_OP_POW3) PPI_UN_CASE(PPI_OP_POW4) PPI_UN_CASE(PPI_OP_POW5)
+      PPI_UN_CASE(PPI_OP_NEG) PPI_UN_CASE(PPI_OP_ROUND) PPI_UN_CASE(PPI_OP_CEIL)
+      PPI_UN_CASE(PPI_OP_FLOOR) PPI_UN_CASE(PPI_OP_EXP) PPI_UN_CASE(PPI_OP_EXP10)
+      PPI_UN_CASE(PPI_OP_EXP2) PPI_UN_CASE(PPI_OP_SIN) PPI_UN_CASE(PPI_OP_COS)
+      PPI_UN_CASE(PPI_OP_STEP) PPI_UN_CASE(PPI_OP_SIGN) PPI_UN_CASE(PPI_OP_LOGISTIC)
+      PPI_UN_CASE(PPI_OP_GAMMA) PPI_UN_CASE(PPI_OP_GAUSS) PPI_UN_CASE(PPI_OP_SQRT)
+      PPI_UN_CASE(PPI_OP_LOG) PPI_UN_CASE(PPI_OP_LOG10) PPI_UN_CASE(PPI_OP_LOG2)
+      PPI_UN_CASE(PPI_OP_TAN)
+#undef PPI_UN_CASE
+
+#define PPI_BIN_CASES(OP)                                                          \
+      case M_BR_L + (OP - PPI_OP_AND): {                                           \
+         float x[R];                                                              \
+         load_row(mine + (size_t)ins.y * T, P, x);                                    \
+         _Pragma("unroll") for (int r = 0; r < R; ++r) acc[r] = binop<OP, MATH>(acc[r], x[r], prot); \
+         break;                                                                    \
+      }                                                                            \
+      case M_BR_R + (OP - PPI_OP_AND): {                                           \
+         float x[R];                                                              \
+         load_row(mine + (size_t)ins.y * T, P, x);                                    \
+         _Pragma("unroll") for (int r = 0; r < R; ++r) acc[r] = binop<OP, MATH>(x[r], acc[r], prot); \
+         break;                                                                    \
+      }                                                                            \
+      case M_BC_L + (OP - PPI_OP_AND): {                                           \
+         const float k = __uint_as_float(ins.y);                                   \
+         _Pragma("unroll") for (int r = 0; r < R; ++r) acc[r] = binop<OP, MATH>(acc[r], k, prot); \
+         break;                                                                    \
+      }                                                                            \
+      case M_BC_R + (OP - PPI_OP_AND): {                                           \
+         const float k = __uint_as_float(ins.y);                                   \
+         _Pragma("unroll") for (int r = 0; r < R; ++r) acc[r] = binop<OP, MATH>(k, acc[r], prot); \
+         break;                                                                    \
+      }
+      PPI_BIN_CASES(PPI_OP_AND) PPI_BIN_CASES(PPI_OP_OR) PPI_BIN_CASES(PPI_OP_XOR)
+      PPI_BIN_CASES(PPI_OP_GREATER) PPI_BIN_CASES(PPI_OP_GREATEREQUAL)
+      PPI_BIN_CASES(PPI_OP_LESS) PPI_BIN_CASES(PPI_OP_LESSEQUAL) PPI_BIN_CASES(PPI_OP_EQUAL)
+      PPI_BIN_CASES(PPI_OP_NOTEQUAL) PPI_BIN_CASES(PPI_OP_ADD) PPI_BIN_CASES(PPI_OP_SUB)
+      PPI_BIN_CASES(PPI_OP_MULT) PPI_BIN_CASES(PPI_OP_MEAN) PPI_BIN_CASES(PPI_OP_MAX)
+      PPI_BIN_CASES(PPI_OP_MIN) PPI_BIN_CASES(PPI_OP_MOD) PPI_BIN_CASES(PPI_OP_POW)
+      PPI_BIN_CASES(PPI_OP_DIV)
+#undef PPI_BIN_CASES
+
+#define PPI_ITE_CASE(PERM)                                                            \
+      case M_ITE + PERM: {                                                            \
+         float ra[R], rb[R];                                                     \
+         load_row(mine + (size_t)(ins.y & 0xFFFFu) * T, P, ra);                       \
+         load_row(mine + (size_t)(ins.y >> 16) * T, P, rb);                           \
+         _Pragma("unroll") for (int r = 0; r < R; ++r) {                          \
+            const float v3[3] = {acc[r], ra[r], rb[r]};                            \
+            acc[r] = truthy(v3[ite_role(PERM, 0)]) ? v3[ite_role(PERM, 1)] : v3[ite_role(PERM, 2)]; \
+         }                                                                         \
+         break;                                                                    \
+      }
+      PPI_ITE_CASE(0) PPI_ITE_CASE(1) PPI_ITE_CASE(2) PPI_ITE_CASE(3) PPI_ITE_CASE(4)
+      PPI_ITE_CASE(5)
+#undef PPI_ITE_CASE
+      default: __builtin_unreachable();
+      }
+      ins = nxt;
+      ++pc;
+   }
+}
+
+// ---- generic stack interpreter ----------------------------------------------
+template <int MATH>
+__device__ __forceinline__ float generic_op(int op, float a, float b, int prot) {
+   switch (op) {
+#define PPI_GU(OP) case OP: return unop<OP, MATH>(a, prot);
+      PPI_GU(PPI_OP_NOT) PPI_GU(PPI_OP_ABS) PPI_GU(PPI_OP_POW2) PPI_GU(PPI_OP_POW3)
+      PPI_GU(PPI_OP_POW4) PPI_GU(PPI_OP_POW5) PPI_GU(PPI_OP_NEG) PPI_GU(PPI_OP_ROUND)
+      PPI_GU(PPI_OP_CEIL) PPI_GU(PPI_OP_FLOOR) PPI_GU(PPI_OP_EXP) PPI_GU(PPI_OP_EXP10)
+      PPI_GU(PPI_OP_EXP2) PPI_GU(PPI_OP_SIN) PPI_GU(PPI_OP_COS) PPI_GU(PPI_OP_STEP)
+      PPI_GU(PPI_OP_SIGN) PPI_GU(PPI_OP_LOGISTIC) PPI_GU(PPI_OP_GAMMA) PPI_GU(PPI_OP_GAUSS)
+      PPI_GU(PPI_OP_SQRT) PPI_GU(PPI_OP_LOG) PPI_GU(PPI_OP_LOG10) PPI_GU(PPI_OP_LOG2)
+      PPI_GU(PPI_OP_TAN)
+#undef PPI_GU
+#define PPI_GB(OP) case OP: return binop<OP, MATH>(a, b, prot);
+      PPI_GB(PPI_OP_AND) PPI_GB(PPI_OP_OR) PPI_GB(PPI_OP_XOR) PPI_GB(PPI_OP_GREATER)
+      PPI_GB(PPI_OP_GREATEREQUAL) PPI_GB(PPI_OP_LESS) PPI_GB(PPI_OP_LESSEQUAL)
+      PPI_GB(PPI_OP_EQUAL) PPI_GB(PPI_OP_NOTEQUAL) PPI_GB(PPI_OP_ADD) PPI_GB(PPI_OP_SUB)
+      PPI_GB(PPI_OP_MULT) PPI_GB(PPI_OP_MEAN) PPI_GB(PPI_OP_MAX) PPI_GB(PPI_OP_MIN)
+      PPI_GB(PPI_OP_MOD) PPI_GB(PPI_OP_POW) PPI_GB(PPI_OP_DIV)
+#undef PPI_GB
+   default: return __uint_as_float(0x7fc00000u);
+   }
+}
+
+// Right-to-left stack evaluation with the reference's stack semantics
+// (accelerator.cl:28-53); missing operands of a malformed program read as NaN.
+template <int MATH, int R>
+__device__ __noinline__ void run_generic(const uint2* __restrict__ code, const float* __restrict__ tile,
+                                         int T, int P, int tid, float* __restrict__ out, int prot) {
+   float stk[kGenericStack];
+   const float qnan = __uint_as_float(0x7fc00000u);
+#pragma unroll 1
+   for (int r = 0; r < R; ++r) {
+      int top = -1;
+      const int rec = tile_pos(tid, r, P);
+#pragma unroll 1
+      for (int pc = 0;; ++pc) {
+         const uint2 ins = code[pc];
+         const int op = (int)ins.x;
+         if (ins.x == kGenericEnd) break;
+         const int ar = op_arity(op);
+         if (top + 1 < ar) {
+            const int have = top + 1, miss = ar - have;
+            for (int k = have - 1; k >= 0; --k) stk[k + miss] = stk[k];
+            for (int k = 0; k < miss; ++k) stk[k] = qnan;
+            top = ar - 1;
+         }
+         if (ar == 0) {
+            float v;
+            if (op == PPI_OP_ATTRIBUTE) v = tile[(size_t)ins.y * T + rec];
+            else v = __uint_as_float(ins.y);   // CONST / LITERAL value, INVALID = NaN
+            stk[++top] = v;
+         } else if (ar == 3) {
+            stk[top - 2] = truthy(stk[top]) ? stk[top - 1] : stk[top - 2];
+            top -= 2;
+         } else if (ar == 2) {
+            stk[top - 1] = generic_op<MATH>(op, stk[top], stk[top - 1], prot);
+            --top;
+         } else {
+            stk[top] = generic_op<MATH>(op, stk[top], 0.0f, prot);
+         }
+      }
+      out[r] = top >= 0 ? stk[top] : qnan;
+   }
+}
+
+__device__ __forceinline__ void stage_tile(const EvalArgs& a, float* s_tile, int base, int T,
+                                           int tid, int P) {
+   const bool vec = (base & 3) == 0;
+   for (int cidx = 0; cidx < a.ncol; ++cidx) {
+      const float* src = a.data + (size_t)cidx * a.ld + base;
+      float* dst = s_tile + (size_t)cidx * T;
+      for (int t = tid * 4; t < T; t += P * 4) {
+         if (vec && base + t + 3 < a.ld) {
+            *reinterpret_cast<float4*>(dst + t) = __ldg(reinterpret_cast<const float4*>(src + t));
+         } else {
+#pragma unroll
+            for (int j = 0; j < 4; ++j) dst[t + j] = (base + t + j < a.ld) ? __ldg(src + t + j) : 0.0f;
+         }
+      }
+   }
+}
+
+__device__ __forceinline__ unsigned long long fitness_key(float f, int prog) {
+   uint32_t u = __float_as_uint(f);
+   u = (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+   return ((unsigned long long)u << 32) | (unsigned long long)(0xFFFFFFFFu - (uint32_t)prog);
+}
+
+__device__ __forceinline__ float reduce1(int reduce_max, float acc, float e, float fnlin) {
+   if (reduce_max) {
+      const float v = e * fnlin;
+      return (v > acc) ? v : acc;
+   }
+   return acc + e;
+}
+
+// __local tree of accelerator.cl:157-167 / 252-262 over L values.
+__device__ __forceinline__ void local_tree(float* pe, int L, int reduce_max, int tid, int P) {
+   int p2 = 1;
+   while (p2 < L) p2 <<= 1;
+   for (int s = p2 >> 1; s > 0; s >>= 1) {
+      for (int l = tid; l < s; l += P)
+         if (l + s < L) pe[l] = reduce_max ? ((pe[l + s] > pe[l]) ? pe[l + s] : pe[l]) : pe[l] + pe[l + s];
+      __syncthreads();
+   }
+}
+
+template <int MATH, int R>
+__global__ void __launch_bounds__(128, 4) eval_kernel(const EvalArgs a) {
+   extern __shared__ __align__(16) unsigned char smem_raw[];
+   __shared__ int s_prog;
+   const int P = blockDim.x, tid = threadIdx.x, T = P * R;
+   const int L = a.lanes;
+   uint2* s_code = reinterpret_cast<uint2*>(smem_raw);
+   float* s_tile = reinterpret_cast<float*>(smem_raw + code_bytes(a.code_stride));
+   const bool aligned = a.strategy == PPI_STRATEGY_PDP && L == T;
+   float* s_err = s_tile + (size_t)(a.ncol + kSlots) * T;
+   // the aligned path needs no error/lane buffers: its final lane values
+   // reuse the start of the rows region once the last tile is done
+   float* s_acc = aligned ? s_tile : s_err + T;
+   int* s_done = reinterpret_cast<int*>(s_acc + L);
+   const bool dp = a.strategy == PPI_STRATEGY_DP;
+   const int Teff = dp ? L * (T / L) : T;
+   const float fnlin = (float)a.nlin;
+
+   for (;;) {
+      if (tid == 0) s_prog = (int)atomicAdd(&a.counters[0], 1u);
+      __syncthreads();
+      const int prog = s_prog;
+      if (prog >= a.n) break;
+      const int2 m = a.meta[prog];
+      const int size = a.size[prog];
+      float fit = FLT_MAX;
+      if (m.x == kKindInvalid || m.x == kKindUnsupported) {
+         // size 0 (sizes outside [1, max_size] are treated as 0)
+         if (tid == 0) {
+            if (m.x == kKindUnsupported) atomicOr(a.status, kStatusUnsupportedProgram);
+            if (m.x == kKindInvalid && dp) {
+               // every group reports MAXFLOAT (accelerator.cl:108-112); host rule
+               float sum = 0.0f;
+               const int G = (a.nlin + L - 1) / L;
+               for (int g = 0; g < G; ++g) sum = reduce1(a.reduce_max, sum, FLT_MAX, fnlin);
+               fit = nonfinite(sum) ? FLT_MAX : sum / fnlin;
+            }
+         }
+      } else {
+         const uint2* g = a.code + (size_t)prog * a.code_stride;
+         for (int i = tid; i < m.y; i += P) s_code[i] = g[i];
+         if (!aligned)
+            for (int l = tid; l < L; l += P) { s_acc[l] = 0.0f; s_done[l] = 0; }
+         float lacc[R];
+#pragma unroll
+         for (int r = 0; r < R; ++r) lacc[r] = 0.0f;
+         uint32_t ldone = 0u;
+         float dsum = 0.0f;
+         bool ddone = false;
+         for (int base = 0; base < a.nlin; base += Teff) {
+            __syncthreads();
+            stage_tile(a, s_tile, base, T, tid, P);
+            __syncthreads();
+            float v[R];
+            if (m.x == kKindFast) {
+               run_fast<MATH, R>(s_code, s_tile + tid * 4, T, P, v, a.prot);
+            } else {
+               float tmp[R];
+               run_generic<MATH, R>(s_code, s_tile, T, P, tid, tmp, a.prot);
+#pragma unroll
+               for (int r = 0; r < R; ++r) v[r] = tmp[r];
+            }
+            float ycol[R];
+            load_row(s_tile + (size_t)(a.ncol - 1) * T + tid * 4, P, ycol);
+            float e[R];
+#pragma unroll
+            for (int r = 0; r < R; ++r) e[r] = apply_error(a.ef, v[r], ycol[r], a.cost, a.cost_n);
+            if (aligned) {
+#pragma unroll
+               for (int r = 0; r < R; ++r) {
+                  const int n = base + tile_pos(tid, r, P);
+                  if (n < a.nlin && !((ldone >> r) & 1u)) {
+                     if (nonfinite(e[r])) { lacc[r] = FLT_MAX; ldone |= 1u << r; }
+                     else lacc[r] = reduce1(a.reduce_max, lacc[r], e[r], fnlin);
+                  }
+               }
+            } else {
+#pragma unroll
+               for (int r = 0; r < R; ++r) {
+                  const int t = tile_pos(tid, r, P);
+                  s_err[t] = (dp && base + t >= a.nlin) ? 0.0f : e[r];
+               }
+               __syncthreads();
+               if (dp) {
+                  const int G = Teff / L;
+                  int p2 = 1;
+                  while (p2 < L) p2 <<= 1;
+                  for (int s = p2 >> 1; s > 0; s >>= 1) {
+                     for (int idx = tid; idx < G * s; idx += P) {
+                        const int gi = idx / s, l = idx - gi * s;
+                        if (l + s < L) {
+                           float* pe = s_err + gi * L;
+                           pe[l] = a.reduce_max ? ((pe[l + s] > pe[l]) ? pe[l + s] : pe[l]) : pe[l] + pe[l + s];
+                        }
+                     }
+                     __syncthreads();
+                  }
+                  if (tid == 0) {
+                     for (int gi = 0; gi < G && !ddone; ++gi) {
+                        if (base + gi * L >= a.nlin) break;
+                        const float part = s_err[gi * L];
+                        if (nonfinite(part)) { dsum = FLT_MAX; ddone = true; }
+                        else dsum = reduce1(a.reduce_max, dsum, part, fnlin);
+                     }
+                  }
+               } else {
+                  const int end = min(base + T, a.nlin);
+                  const int off = base % L;
+                  for (int l = tid; l < L; l += P) {
+                     if (s_done[l]) continue;
+                     float acc = s_acc[l];
+                     int done = 0;
+                     for (int n = base + (l - off + L) % L; n < end; n += L) {
+                        const float ev = s_err[n - base];
+                        if (nonfinite(ev)) { acc = FLT_MAX; done = 1; break; }
+                        acc = reduce1(a.reduce_max, acc, ev, fnlin);
+                     }
+                     s_acc[l] = acc;
+                     if (done) s_done[l] = 1;
+                  }
+               }
+            }
+         }
+         __syncthreads();
+         if (dp) {
+            if (tid == 0) fit = nonfinite(dsum) ? FLT_MAX : dsum / fnlin + a.alpha * (float)size;
+         } else {
+            if (aligned) {
+               __syncthreads();   // every thread is done with the rows region
+#pragma unroll
+               for (int r = 0; r < R; ++r) s_acc[tile_pos(tid, r, P)] = lacc[r];
+               __syncthreads();
+            }
+            local_tree(s_acc, L, a.reduce_max, tid, P);
+            if (tid == 0) {
+               const float pe = s_acc[0];
+               const float vv = nonfinite(pe) ? FLT_MAX : pe / fnlin;
+               fit = vv + a.alpha * (float)size;
+            }
+         }
+      }
+      if (tid == 0) {
+         a.fitness[prog] = fit;
+         atomicMin(a.best_key, fitness_key(fit, prog));
+      }
+      __syncthreads();
+   }
+   if (tid == 0) {
+      __threadfence();
+      const unsigned done = atomicAdd(&a.counters[1], 1u);
+      if (done == gridDim.x - 1) {
+         __threadfence();
+         const unsigned long long k = *reinterpret_cast<volatile unsigned long long*>(a.best_key);
+         a.best_index[0] = (int32_t)(0xFFFFFFFFu - (uint32_t)(k & 0xFFFFFFFFull));
+      }
+   }
+}
+
+// Per-record predictions of program 0 (ppp prediction mode).
+template <int MATH, int R>
+__global__ void __launch_bounds__(128, 4) predict_kernel(const PredictArgs a) {
+   extern __shared__ __align__(16) unsigned char smem_raw[];
+   const int P = blockDim.x, tid = threadIdx.x, T = P * R;
+   const int2 m = a.meta[0];
+   uint2* s_code = reinterpret_cast<uint2*>(smem_raw);
+   float* s_tile = reinterpret_cast<float*>(smem_raw + code_bytes(m.y));
+   for (int i = tid; i < m.y; i += P) s_code[i] = a.code[i];
+   EvalArgs ea{};
+   ea.data = a.data;
+   ea.nlin = a.nlin;
+   ea.ncol = a.ncol;
+   ea.ld = a.ld;
+   for (int base = blockIdx.x * T; base < a.nlin; base += gridDim.x * T) {
+      __syncthreads();
+      stage_tile(ea, s_tile, base, T, tid, P);
+      __syncthreads();
+      float v[R];
+      if (m.x == kKindFast) {
+         run_fast<MATH, R>(s_code, s_tile + tid * 4, T, P, v, a.prot);
+      } else if (m.x == kKindGeneric) {
+         float tmp[R];
+         run_generic<MATH, R>(s_code, s_tile, T, P, tid, tmp, a.prot);
+#pragma unroll
+         for (int r = 0; r < R; ++r) v[r] = tmp[r];
+      } else {
+#pragma unroll
+         for (int r = 0; r < R; ++r) v[r] = __uint_as_float(0x7fc00000u);
+      }
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+         const int n = base + tile_pos(tid, r, P);
+         if (n < a.nlin) a.out[n] = v[r];
+      }
+   }
+}
+
+
+template <int MATH, int R>
+cudaError_t configure_t() {
+   cudaError_t e = cudaFuncSetAttribute(eval_kernel<MATH, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+   if (e != cudaSuccess) return e;
+   return cudaFuncSetAttribute(predict_kernel<MATH, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+}
+
+// Per-math entry points, instantiated in evaluate_<math>.cu.
+template <int MATH>
+struct Launch {
+   static cudaError_t evaluate(int R, const EvalArgs& a, int block, int grid, size_t smem, cudaStream_t s) {
+      cudaError_t e = R == 16 ? configure_t<MATH, 16>() : configure_t<MATH, 8>();
+      if (e != cudaSuccess) return e;
+      if (R == 16) eval_kernel<MATH, 16><<<grid, block, smem, s>>>(a);
+      else eval_kernel<MATH, 8><<<grid, block, smem, s>>>(a);
+      return cudaGetLastError();
+   }
+   static cudaError_t predict(int R, const PredictArgs& a, int block, int grid, size_t smem, cudaStream_t s) {
+      cudaError_t e = R == 16 ? configure_t<MATH, 16>() : configure_t<MATH, 8>();
+      if (e != cudaSuccess) return e;
+      if (R == 16) predict_kernel<MATH, 16><<<grid, block, smem, s>>>(a);
+      else predict_kernel<MATH, 8><<<grid, block, smem, s>>>(a);
+      return cudaGetLastError();
+   }
+   static cudaError_t occupancy(int R, int block, size_t smem, int* per_sm) {
+      cudaError_t e = R == 16 ? configure_t<MATH, 16>() : configure_t<MATH, 8>();
+      if (e != cudaSuccess) return e;
+      if (R == 16) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, eval_kernel<MATH, 16>, block, smem);
+      return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, eval_kernel<MATH, 8>, block, smem);
+   }
+};
+
+}  // namespace ev
+}  // namespace ppi

@@ -1,0 +1,16 @@
+// evaluate_parity.cu -- evaluator kernels instantiated for one math mode
+// (separate translation units so that the build compiles them in parallel).
+#include "evaluate_impl.cuh"
+
+namespace ppi {
+template struct ev::Launch<kMathParity>;
+cudaError_t launch_evaluate_parity(int R, const EvalArgs& a, int block, int grid, size_t smem, cudaStream_t s) {
+   return ev::Launch<kMathParity>::evaluate(R, a, block, grid, smem, s);
+}
+cudaError_t launch_predict_parity(int R, const PredictArgs& a, int block, int grid, size_t smem, cudaStream_t s) {
+   return ev::Launch<kMathParity>::predict(R, a, block, grid, smem, s);
+}
+cudaError_t evaluate_occupancy_parity(int R, int block, size_t smem, int* per_sm) {
+   return ev::Launch<kMathParity>::occupancy(R, block, smem, per_sm);
+}
+}  // namespace ppi

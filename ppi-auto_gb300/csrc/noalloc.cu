@@ -125,29 +125,10 @@ extern "C" ppi_status ppi_gpu_evaluate_noalloc(const ppi_gpu_config* c, const fl
    int sm_count = 0;
    if (cudaDeviceGetAttribute(&sm_count, cudaDevAttrMultiProcessorCount, c->device) != cudaSuccess)
       return PPI_ERR_CUDA;
-   int L = c->lanes;
-   if (c->strategy == PPI_STRATEGY_PP) L = 1;
-   else if (L <= 0 && c->strategy == PPI_STRATEGY_PDP) L = nlin < 1024 ? nlin : 1024;
-   else if (L <= 0) L = std::min(1024, (int)std::ceil(nlin / (float)std::max(1, sm_count)));
-   else if (c->strategy == PPI_STRATEGY_PDP) L = std::min(L, (int)nlin);
-   if (L < 1 || L > kMaxLanes) return PPI_ERR_UNSUPPORTED;
-   int P;
-   if (c->strategy == PPI_STRATEGY_PDP && L % (32 * kR) == 0 && L / kR <= 128) {
-      P = L / kR;
-   } else {
-      const int need = (c->strategy == PPI_STRATEGY_DP) ? L : std::min((int)nlin, 128 * kR);
-      P = std::min(128, std::max(32, ((need + kR - 1) / kR + 31) / 32 * 32));
-   }
-   if (c->strategy == PPI_STRATEGY_DP && L > P * kR) return PPI_ERR_UNSUPPORTED;
-   size_t smem = evaluate_smem_bytes(code_stride, ncol, P, L);
-   while (smem > 200 * 1024 && P > 32 && !(c->strategy == PPI_STRATEGY_DP && L > (P / 2) * kR)) {
-      P /= 2;
-      smem = evaluate_smem_bytes(code_stride, ncol, P, L);
-   }
-   if (smem > 200 * 1024) return PPI_ERR_UNSUPPORTED;
-   int per_sm = 0;
-   if (evaluate_occupancy(c->math, P, smem, &per_sm) != cudaSuccess || per_sm < 1) return PPI_ERR_CUDA;
-   const int grid = std::max(1, std::min((int)n, per_sm * sm_count));
+   Geometry g;
+   const int L = resolve_lanes(c->strategy, c->lanes, nlin, sm_count);
+   if (plan_geometry(c->strategy, L, c->math, nlin, ncol, code_stride, n, sm_count, &g))
+      return PPI_ERR_UNSUPPORTED;
 
    unsigned char* base = nullptr;
    ppi_status st = scratch_base(c->device, &base);
@@ -178,13 +159,14 @@ extern "C" ppi_status ppi_gpu_evaluate_noalloc(const ppi_gpu_config* c, const fl
    t.max_size = c->max_size; t.ncol = ncol; t.lut = lut; t.lut_min = mn; t.lut_len = lut_len;
    t.code = code; t.code_stride = code_stride; t.meta = meta; t.work = work;
    t.best_key = key; t.counters = counters; t.status = status;
+   t.prot = c->protected_fns ? 1 : 0; t.fold = 1;
    EvalArgs e{};
    e.data = d_data; e.nlin = nlin; e.ncol = ncol; e.ld = ld; e.code = code;
    e.code_stride = code_stride; e.meta = meta; e.size = d_size; e.n = n; e.alpha = alpha;
    e.ef = c->error_fn; e.reduce_max = c->reduce_max ? 1 : 0; e.prot = c->protected_fns ? 1 : 0;
-   e.cost = cost; e.cost_n = c->cost_n; e.strategy = c->strategy; e.lanes = L; e.fitness = d_fitness;
+   e.cost = cost; e.cost_n = c->cost_n; e.strategy = c->strategy; e.lanes = g.lanes; e.fitness = d_fitness;
    e.best_key = key; e.counters = counters; e.best_index = d_best_index; e.status = status;
-   if (launch_translate(t, s) != cudaSuccess) return PPI_ERR_CUDA;
-   if (launch_evaluate(c->math, e, P, grid, smem, s) != cudaSuccess) return PPI_ERR_CUDA;
+   if (launch_translate(c->math, t, s) != cudaSuccess) return PPI_ERR_CUDA;
+   if (launch_evaluate(c->math, g.R, e, g.block, g.grid, g.smem, s) != cudaSuccess) return PPI_ERR_CUDA;
    return PPI_OK;
 }

@@ -32,8 +32,8 @@ struct ppi_gpu {
    float* d_data = nullptr;
    int nlin = 0, ncol = 0, ld = 0;
    bool have_data = false;
-   int lanes = 1, block = 128, grid = 1;
-   size_t smem = 0;
+   int lanes = 1;
+   Geometry geo;
    // per-generation buffers (capacity population_size)
    int32_t* d_ph = nullptr;
    float* d_eph = nullptr;
@@ -105,29 +105,11 @@ void free_all(ppi_gpu* h) {
 
 // Evaluator geometry for the current dataset and lane count.
 ppi_status plan(ppi_gpu* h) {
-   const int L = h->lanes;
-   int P;
-   if (h->cfg.strategy == PPI_STRATEGY_PDP && L % (32 * kR) == 0 && L / kR <= 128) {
-      P = L / kR;   // lane == tile position: register accumulation
-   } else {
-      const int need = (h->cfg.strategy == PPI_STRATEGY_DP) ? L : std::min(h->nlin, 128 * kR);
-      P = std::min(128, std::max(32, ((need + kR - 1) / kR + 31) / 32 * 32));
-   }
-   if (h->cfg.strategy == PPI_STRATEGY_DP && L > P * kR)
-      return fail(h, PPI_ERR_UNSUPPORTED, "DP lanes above 1024 records per group are not supported");
-   size_t smem = evaluate_smem_bytes(h->code_stride, h->ncol, P, L);
-   while (smem > 200 * 1024 && P > 32 && !(h->cfg.strategy == PPI_STRATEGY_DP && L > (P / 2) * kR)) {
-      P /= 2;
-      smem = evaluate_smem_bytes(h->code_stride, h->ncol, P, L);
-   }
-   if (smem > 200 * 1024)
-      return fail(h, PPI_ERR_UNSUPPORTED, "dataset has too many columns for one shared-memory tile");
-   int per_sm = 0;
-   PPI_CUDA(h, evaluate_occupancy(h->cfg.math, P, smem, &per_sm));
-   if (per_sm < 1) return fail(h, PPI_ERR_UNSUPPORTED, "evaluator does not fit on an SM");
-   h->block = P;
-   h->smem = smem;
-   h->grid = std::max(1, std::min(h->cfg.population_size, per_sm * h->sm_count));
+   Geometry g;
+   const char* why = plan_geometry(h->cfg.strategy, h->lanes, h->cfg.math, h->nlin, h->ncol,
+                                   h->code_stride, h->cfg.population_size, h->sm_count, &g);
+   if (why) return fail(h, PPI_ERR_UNSUPPORTED, why);
+   h->geo = g;
    return PPI_OK;
 }
 
@@ -148,6 +130,7 @@ ppi_status enqueue(ppi_gpu* h, const int32_t* d_ph, const float* d_eph, const in
    t.lut = h->d_lut; t.lut_min = h->lut_min; t.lut_len = h->lut_len;
    t.code = h->d_code; t.code_stride = h->code_stride; t.meta = h->d_meta; t.work = h->d_work;
    t.best_key = h->d_key; t.counters = h->d_counters; t.status = h->d_status;
+   t.prot = h->cfg.protected_fns ? 1 : 0; t.fold = 1;
    EvalArgs e{};
    e.data = h->d_data; e.nlin = h->nlin; e.ncol = h->ncol; e.ld = h->ld;
    e.code = h->d_code; e.code_stride = h->code_stride; e.meta = h->d_meta; e.size = d_size;
@@ -156,9 +139,10 @@ ppi_status enqueue(ppi_gpu* h, const int32_t* d_ph, const float* d_eph, const in
    e.strategy = h->cfg.strategy; e.lanes = h->lanes; e.fitness = d_fit; e.best_key = h->d_key;
    e.counters = h->d_counters; e.best_index = d_best; e.status = h->d_status;
    PPI_CUDA(h, cudaEventRecord(h->ev0, s));
-   PPI_CUDA(h, launch_translate(t, s));
+   PPI_CUDA(h, launch_translate(h->cfg.math, t, s));
    PPI_CUDA(h, cudaEventRecord(h->evm, s));
-   PPI_CUDA(h, launch_evaluate(h->cfg.math, e, h->block, std::min(h->grid, n), h->smem, s));
+   PPI_CUDA(h, launch_evaluate(h->cfg.math, h->geo.R, e, h->geo.block, std::min(h->geo.grid, n),
+                               h->geo.smem, s));
    PPI_CUDA(h, cudaEventRecord(h->ev1, s));
    h->last_launches = 2;
    return PPI_OK;
@@ -279,13 +263,7 @@ ppi_status ppi_gpu_set_dataset(ppi_gpu* h, const float* const* rows, int32_t nli
    h->nlin = nlin;
    h->ncol = ncol;
    h->ld = ld;
-   // Lane count: -cl-mls when given; else the reference's rule on a device
-   // with 1024-wide work-groups and 152 compute units (accelerator.cc:296-330).
-   int L = h->cfg.lanes;
-   if (h->cfg.strategy == PPI_STRATEGY_PP) L = 1;
-   else if (L <= 0 && h->cfg.strategy == PPI_STRATEGY_PDP) L = std::min(nlin, 1024);
-   else if (L <= 0) L = std::min(1024, (int)std::ceil(nlin / (float)std::max(1, h->sm_count)));
-   else if (h->cfg.strategy == PPI_STRATEGY_PDP) L = std::min(L, nlin);
+   const int L = resolve_lanes(h->cfg.strategy, h->cfg.lanes, nlin, h->sm_count);
    if (L < 1 || L > kMaxLanes) return fail(h, PPI_ERR_UNSUPPORTED, "lane count out of range");
    h->lanes = L;
    ppi_status s = plan(h);
@@ -368,21 +346,23 @@ ppi_status ppi_gpu_predict(ppi_gpu* h, const int32_t* ph, const float* eph, int3
    t.lut = h->d_lut; t.lut_min = h->lut_min; t.lut_len = h->lut_len;
    t.code = h->d_code; t.code_stride = h->code_stride; t.meta = h->d_meta; t.work = h->d_work;
    t.best_key = h->d_key; t.counters = h->d_counters; t.status = h->d_status;
+   t.prot = h->cfg.protected_fns ? 1 : 0; t.fold = 1;
    PredictArgs p{};
    p.data = h->d_data; p.nlin = h->nlin; p.ncol = h->ncol; p.ld = h->ld;
    p.code = h->d_code; p.meta = h->d_meta; p.prot = h->cfg.protected_fns ? 1 : 0; p.out = h->d_pred;
+   const int R = 8;
    int P = 128;
-   size_t smem = evaluate_smem_bytes(h->code_stride, h->ncol, P, 0);
+   size_t smem = evaluate_smem_bytes(h->code_stride, h->ncol, P, R, 0, false);
    while (smem > 200 * 1024 && P > 32) {
       P /= 2;
-      smem = evaluate_smem_bytes(h->code_stride, h->ncol, P, 0);
+      smem = evaluate_smem_bytes(h->code_stride, h->ncol, P, R, 0, false);
    }
    if (smem > 200 * 1024) return fail(h, PPI_ERR_UNSUPPORTED, "too many columns");
-   const int tiles = (h->nlin + P * kR - 1) / (P * kR);
+   const int tiles = (h->nlin + P * R - 1) / (P * R);
    const int grid = std::max(1, std::min(tiles, 4 * h->sm_count));
    PPI_CUDA(h, cudaEventRecord(h->ev0, h->stream));
-   PPI_CUDA(h, launch_translate(t, h->stream));
-   PPI_CUDA(h, launch_predict(h->cfg.math, p, P, grid, smem, h->stream));
+   PPI_CUDA(h, launch_translate(h->cfg.math, t, h->stream));
+   PPI_CUDA(h, launch_predict(h->cfg.math, R, p, P, grid, smem, h->stream));
    PPI_CUDA(h, cudaEventRecord(h->ev1, h->stream));
    PPI_CUDA(h, cudaMemcpyAsync(out, h->d_pred, (size_t)h->nlin * 4, cudaMemcpyDeviceToHost, h->stream));
    PPI_CUDA(h, cudaStreamSynchronize(h->stream));

@@ -251,6 +251,8 @@ struct TranslateArgs {
    unsigned long long* best_key;
    unsigned* counters;         // [0] work queue, [1] finished blocks
    int* status;
+   int prot;                   // PROTECTED, for constant folding
+   int fold;                   // fold constant subexpressions
 };
 
 struct EvalArgs {
@@ -282,13 +284,24 @@ struct PredictArgs {
    float* out;
 };
 
+// Evaluator launch geometry: lanes, block size P, records per thread R,
+// dynamic shared memory and a one-wave persistent grid.
+struct Geometry {
+   int lanes = 1, block = 128, R = 8, grid = 1;
+   size_t smem = 0;
+};
+int resolve_lanes(int strategy, int lanes, int nlin, int sm_count);
+// Returns nullptr on success, else why the configuration is unsupported.
+const char* plan_geometry(int strategy, int lanes, int math, int nlin, int ncol, int code_stride,
+                          int n_max, int sm_count, Geometry* g);
+
 // Kernel launchers (evaluate.cu / translate.cu).
-cudaError_t launch_translate(const TranslateArgs& a, cudaStream_t s);
-cudaError_t launch_evaluate(int math, const EvalArgs& a, int block, int grid, size_t smem,
+cudaError_t launch_translate(int math, const TranslateArgs& a, cudaStream_t s);
+cudaError_t launch_evaluate(int math, int R, const EvalArgs& a, int block, int grid, size_t smem,
                             cudaStream_t s);
-cudaError_t launch_predict(int math, const PredictArgs& a, int block, int grid, size_t smem,
+cudaError_t launch_predict(int math, int R, const PredictArgs& a, int block, int grid, size_t smem,
                            cudaStream_t s);
-cudaError_t evaluate_occupancy(int math, int block, size_t smem, int* blocks_per_sm);
-size_t evaluate_smem_bytes(int code_stride, int ncol, int block, int lanes);
+cudaError_t evaluate_occupancy(int math, int R, int block, size_t smem, int* blocks_per_sm);
+size_t evaluate_smem_bytes(int code_stride, int ncol, int block, int R, int lanes, bool aligned);
 
 }  // namespace ppi

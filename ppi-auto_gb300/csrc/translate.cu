@@ -12,6 +12,11 @@
 //    which independent subtrees are evaluated does not change any value: every
 //    node computes exactly the reference's operation on exactly the
 //    reference's operands.
+// Pass 1 also folds constant subexpressions: an operator whose operands are
+// all constants (CONST, literal, or already folded) becomes a literal whose
+// value is computed here with the same device functions (unop/binop) and the
+// same math mode the evaluator uses, so the folded value is bit-identical to
+// what every record would compute.
 // Malformed programs (too few operands, or more than one value left) and
 // programs needing more than kSlots registers get the generic form instead:
 // the mapped tokens in evaluation order, run by a stack interpreter with the
@@ -36,6 +41,55 @@ __device__ __forceinline__ uint32_t frame(int node, int d, int st) {
    return (uint32_t)node | ((uint32_t)d << 16) | ((uint32_t)st << 24);
 }
 
+// Symbol -> (op, immediate): literal value, constant, or validated column.
+__device__ __forceinline__ void map_token(const TranslateArgs& a, int sym, float e, int* op_out,
+                                          uint32_t* imm_out) {
+   const uint32_t qnan = 0x7fc00000u;
+   int op = PPI_OP_INVALID;
+   uint32_t imm = qnan;
+   const int li = sym - a.lut_min;
+   if (li >= 0 && li < a.lut_len) {
+      const int2 ent = a.lut[li];
+      op = ent.x;
+      if (op == PPI_OP_LITERAL) imm = (uint32_t)ent.y;
+      else if (op == PPI_OP_CONST) imm = __float_as_uint(e);
+      else if (op == PPI_OP_ATTRIBUTE) {
+         if (e >= 0.0f && e < (float)a.ncol) imm = (uint32_t)(int)e;
+         else { op = PPI_OP_INVALID; imm = qnan; }   // defined as NaN (see ppi_gpu.h)
+      }
+   }
+   *op_out = op;
+   *imm_out = imm;
+}
+
+// Value of op applied to constant operands, in math mode MATH.
+template <int MATH>
+__device__ float fold(int op, float x0, float x1, float x2, int prot) {
+   switch (op) {
+#define PPI_FU(OP) case OP: return unop<OP, MATH>(x0, prot);
+      PPI_FU(PPI_OP_NOT) PPI_FU(PPI_OP_ABS) PPI_FU(PPI_OP_POW2) PPI_FU(PPI_OP_POW3)
+      PPI_FU(PPI_OP_POW4) PPI_FU(PPI_OP_POW5) PPI_FU(PPI_OP_NEG) PPI_FU(PPI_OP_ROUND)
+      PPI_FU(PPI_OP_CEIL) PPI_FU(PPI_OP_FLOOR) PPI_FU(PPI_OP_EXP) PPI_FU(PPI_OP_EXP10)
+      PPI_FU(PPI_OP_EXP2) PPI_FU(PPI_OP_SIN) PPI_FU(PPI_OP_COS) PPI_FU(PPI_OP_STEP)
+      PPI_FU(PPI_OP_SIGN) PPI_FU(PPI_OP_LOGISTIC) PPI_FU(PPI_OP_GAMMA) PPI_FU(PPI_OP_GAUSS)
+      PPI_FU(PPI_OP_SQRT) PPI_FU(PPI_OP_LOG) PPI_FU(PPI_OP_LOG10) PPI_FU(PPI_OP_LOG2)
+      PPI_FU(PPI_OP_TAN)
+#undef PPI_FU
+#define PPI_FB(OP) case OP: return binop<OP, MATH>(x0, x1, prot);
+      PPI_FB(PPI_OP_AND) PPI_FB(PPI_OP_OR) PPI_FB(PPI_OP_XOR) PPI_FB(PPI_OP_GREATER)
+      PPI_FB(PPI_OP_GREATEREQUAL) PPI_FB(PPI_OP_LESS) PPI_FB(PPI_OP_LESSEQUAL)
+      PPI_FB(PPI_OP_EQUAL) PPI_FB(PPI_OP_NOTEQUAL) PPI_FB(PPI_OP_ADD) PPI_FB(PPI_OP_SUB)
+      PPI_FB(PPI_OP_MULT) PPI_FB(PPI_OP_MEAN) PPI_FB(PPI_OP_MAX) PPI_FB(PPI_OP_MIN)
+      PPI_FB(PPI_OP_MOD) PPI_FB(PPI_OP_POW) PPI_FB(PPI_OP_DIV)
+#undef PPI_FB
+   case PPI_OP_IF_THEN_ELSE: return truthy(x0) ? x1 : x2;
+   default: return __uint_as_float(0x7fc00000u);
+   }
+}
+
+__device__ __forceinline__ bool is_const_leaf(int op) { return op == PPI_OP_CONST || op == PPI_OP_LITERAL; }
+
+template <int MATH>
 __global__ void translate_kernel(const TranslateArgs a) {
    if (blockIdx.x == 0 && threadIdx.x == 0) {
       *a.best_key = ~0ull;
@@ -55,33 +109,38 @@ __global__ void translate_kernel(const TranslateArgs a) {
    uint2* w = a.work + (size_t)i * 2 * a.max_size;
    uint32_t* frames = reinterpret_cast<uint32_t*>(w + a.max_size);
    uint2* code = a.code + (size_t)i * a.code_stride;
-   const uint32_t qnan = 0x7fc00000u;
 
    // ---- pass 1 -----------------------------------------------------------
    int depth = 0, stack_need = 0;
    bool malformed = false;
    for (int k = sz - 1; k >= 0; --k) {
-      const int sym = ph[k];
-      int op = PPI_OP_INVALID;
-      uint32_t imm = qnan;
-      const int li = sym - a.lut_min;
-      if (li >= 0 && li < a.lut_len) {
-         const int2 e = a.lut[li];
-         op = e.x;
-         if (op == PPI_OP_LITERAL) imm = (uint32_t)e.y;
-         else if (op == PPI_OP_CONST) imm = __float_as_uint(eph[k]);
-         else if (op == PPI_OP_ATTRIBUTE) {
-            const float v = eph[k];
-            if (v >= 0.0f && v < (float)a.ncol) imm = (uint32_t)(int)v;
-            else { op = PPI_OP_INVALID; imm = qnan; }   // defined as NaN (see ppi_gpu.h)
-         }
-      }
+      int op;
+      uint32_t imm;
+      map_token(a, ph[k], eph[k], &op, &imm);
       const int ar = op_arity(op);
       int before = depth;
       if (before < ar) { malformed = true; before = ar; }   // missing operands read as NaN
       depth = before - ar + 1;
       stack_need = max(stack_need, max(before, depth));
       int need = 0, sub = 1;
+      if (!malformed && ar > 0 && a.fold) {
+         // children: c0 = k+1, c1 after c0's subtree, c2 after c1's
+         const int c0 = k + 1;
+         const int c1 = ar > 1 ? c0 + node_sub(w[c0]) : c0;
+         const int c2 = ar > 2 ? c1 + node_sub(w[c1]) : c1;
+         bool all_const = is_const_leaf(node_op(w[c0]));
+         if (ar > 1) all_const = all_const && is_const_leaf(node_op(w[c1]));
+         if (ar > 2) all_const = all_const && is_const_leaf(node_op(w[c2]));
+         if (all_const) {
+            const float v = fold<MATH>(op, __uint_as_float(w[c0].y), __uint_as_float(w[c1].y),
+                                       __uint_as_float(w[c2].y), a.prot);
+            int s = 1 + node_sub(w[c0]);
+            if (ar > 1) s += node_sub(w[c1]);
+            if (ar > 2) s += node_sub(w[c2]);
+            w[k] = node_pack(PPI_OP_LITERAL, 0, s, __float_as_uint(v));
+            continue;
+         }
+      }
       if (!malformed && ar > 0) {
          const int c0 = k + 1;
          const uint2 w0 = w[c0];
@@ -219,9 +278,11 @@ __global__ void translate_kernel(const TranslateArgs a) {
       a.meta[i] = make_int2(kKindUnsupported, 0);
       return;
    }
-   for (int k = sz - 1; k >= 0; --k) {
-      const uint2 wn = w[k];
-      code[sz - 1 - k] = make_uint2((uint32_t)node_op(wn), wn.y);
+   for (int k = sz - 1; k >= 0; --k) {   // the original tokens: nothing folded
+      int op;
+      uint32_t imm;
+      map_token(a, ph[k], eph[k], &op, &imm);
+      code[sz - 1 - k] = make_uint2((uint32_t)op, imm);
    }
    code[sz] = make_uint2(kGenericEnd, 0u);
    a.meta[i] = make_int2(kKindGeneric, sz + 1);
@@ -229,10 +290,12 @@ __global__ void translate_kernel(const TranslateArgs a) {
 
 }  // namespace
 
-cudaError_t launch_translate(const TranslateArgs& a, cudaStream_t s) {
+cudaError_t launch_translate(int math, const TranslateArgs& a, cudaStream_t s) {
    const int block = 128;
    const int grid = max(1, (a.n + block - 1) / block);
-   translate_kernel<<<grid, block, 0, s>>>(a);
+   if (math == kMathParity) translate_kernel<kMathParity><<<grid, block, 0, s>>>(a);
+   else if (math == kMathNative) translate_kernel<kMathNative><<<grid, block, 0, s>>>(a);
+   else translate_kernel<kMathFast><<<grid, block, 0, s>>>(a);
    return cudaGetLastError();
 }
 

