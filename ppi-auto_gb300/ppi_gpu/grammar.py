@@ -272,6 +272,7 @@ def symbol_map_header(g: Grammar, guard="PPI_SYMBOL_MAP") -> str:
     t = g.symbol_table()
     names = {v: k for k, v in g.symbols.items()}
     for sym, op, val in t:
-        lines.append("   { %s, PPI_OP_%s, %.9gf }," % (names[sym], OPS[op], val))
+        lit = float(np.float32(val)).hex() + "f"      # exact: hexadecimal float literal
+        lines.append("   { %s, PPI_OP_%s, %s }," % (names[sym], OPS[op], lit))
     lines += ["};", "#endif", ""]
     return "\n".join(lines)
