@@ -8,15 +8,15 @@
 
 namespace ppi {
 
-cudaError_t launch_evaluate_fast(int R, const EvalArgs& a, int block, int grid, size_t smem, cudaStream_t s);
-cudaError_t launch_evaluate_parity(int R, const EvalArgs& a, int block, int grid, size_t smem, cudaStream_t s);
-cudaError_t launch_evaluate_native(int R, const EvalArgs& a, int block, int grid, size_t smem, cudaStream_t s);
-cudaError_t launch_predict_fast(int R, const PredictArgs& a, int block, int grid, size_t smem, cudaStream_t s);
-cudaError_t launch_predict_parity(int R, const PredictArgs& a, int block, int grid, size_t smem, cudaStream_t s);
-cudaError_t launch_predict_native(int R, const PredictArgs& a, int block, int grid, size_t smem, cudaStream_t s);
-cudaError_t evaluate_occupancy_fast(int R, int block, size_t smem, int* per_sm);
-cudaError_t evaluate_occupancy_parity(int R, int block, size_t smem, int* per_sm);
-cudaError_t evaluate_occupancy_native(int R, int block, size_t smem, int* per_sm);
+cudaError_t launch_evaluate_fast(int opset, const EvalArgs& a, int block, int grid, size_t smem, cudaStream_t s);
+cudaError_t launch_evaluate_parity(int opset, const EvalArgs& a, int block, int grid, size_t smem, cudaStream_t s);
+cudaError_t launch_evaluate_native(int opset, const EvalArgs& a, int block, int grid, size_t smem, cudaStream_t s);
+cudaError_t launch_predict_fast(int opset, const PredictArgs& a, int block, int grid, size_t smem, cudaStream_t s);
+cudaError_t launch_predict_parity(int opset, const PredictArgs& a, int block, int grid, size_t smem, cudaStream_t s);
+cudaError_t launch_predict_native(int opset, const PredictArgs& a, int block, int grid, size_t smem, cudaStream_t s);
+cudaError_t evaluate_occupancy_fast(int opset, int block, size_t smem, int* per_sm);
+cudaError_t evaluate_occupancy_parity(int opset, int block, size_t smem, int* per_sm);
+cudaError_t evaluate_occupancy_native(int opset, int block, size_t smem, int* per_sm);
 
 size_t evaluate_smem_bytes(int code_stride, int ncol, int block, int R, int lanes, bool aligned) {
    const size_t T = (size_t)block * R;
@@ -26,30 +26,45 @@ size_t evaluate_smem_bytes(int code_stride, int ncol, int block, int R, int lane
    return code + rows + T * 4 + (size_t)lanes * 8;
 }
 
-cudaError_t launch_evaluate(int math, int R, const EvalArgs& a, int block, int grid, size_t smem,
+cudaError_t launch_evaluate(int math, int opset, const EvalArgs& a, int block, int grid, size_t smem,
                             cudaStream_t s) {
    switch (math) {
-   case kMathParity: return launch_evaluate_parity(R, a, block, grid, smem, s);
-   case kMathNative: return launch_evaluate_native(R, a, block, grid, smem, s);
-   default: return launch_evaluate_fast(R, a, block, grid, smem, s);
+   case kMathParity: return launch_evaluate_parity(opset, a, block, grid, smem, s);
+   case kMathNative: return launch_evaluate_native(opset, a, block, grid, smem, s);
+   default: return launch_evaluate_fast(opset, a, block, grid, smem, s);
    }
 }
 
-cudaError_t launch_predict(int math, int R, const PredictArgs& a, int block, int grid, size_t smem,
+cudaError_t launch_predict(int math, int opset, const PredictArgs& a, int block, int grid, size_t smem,
                            cudaStream_t s) {
    switch (math) {
-   case kMathParity: return launch_predict_parity(R, a, block, grid, smem, s);
-   case kMathNative: return launch_predict_native(R, a, block, grid, smem, s);
-   default: return launch_predict_fast(R, a, block, grid, smem, s);
+   case kMathParity: return launch_predict_parity(opset, a, block, grid, smem, s);
+   case kMathNative: return launch_predict_native(opset, a, block, grid, smem, s);
+   default: return launch_predict_fast(opset, a, block, grid, smem, s);
    }
 }
 
-cudaError_t evaluate_occupancy(int math, int R, int block, size_t smem, int* per_sm) {
+cudaError_t evaluate_occupancy(int math, int opset, int block, size_t smem, int* per_sm) {
    switch (math) {
-   case kMathParity: return evaluate_occupancy_parity(R, block, smem, per_sm);
-   case kMathNative: return evaluate_occupancy_native(R, block, smem, per_sm);
-   default: return evaluate_occupancy_fast(R, block, smem, per_sm);
+   case kMathParity: return evaluate_occupancy_parity(opset, block, smem, per_sm);
+   case kMathNative: return evaluate_occupancy_native(opset, block, smem, per_sm);
+   default: return evaluate_occupancy_fast(opset, block, smem, per_sm);
    }
+}
+
+int opset_for(const ppi_symbol_entry* symbols, int n) {
+   for (int i = 0; i < n; ++i) {
+      switch (symbols[i].op) {
+      case PPI_OP_INVALID: case PPI_OP_ATTRIBUTE: case PPI_OP_CONST: case PPI_OP_LITERAL:
+      case PPI_OP_ADD: case PPI_OP_SUB: case PPI_OP_MULT: case PPI_OP_DIV:
+      case PPI_OP_ABS: case PPI_OP_POW2: case PPI_OP_NEG: case PPI_OP_EXP: case PPI_OP_SIN:
+      case PPI_OP_COS: case PPI_OP_SQRT: case PPI_OP_LOG:
+         break;
+      default:
+         return kOpsetFull;
+      }
+   }
+   return kOpsetArith;
 }
 
 int resolve_lanes(int strategy, int lanes, int nlin, int sm_count) {
@@ -62,24 +77,19 @@ int resolve_lanes(int strategy, int lanes, int nlin, int sm_count) {
    return lanes;
 }
 
-const char* plan_geometry(int strategy, int lanes, int math, int nlin, int ncol, int code_stride,
-                          int n_max, int sm_count, Geometry* g) {
+const char* plan_geometry(int strategy, int lanes, int math, int opset, int nlin, int ncol,
+                          int code_stride, int n_max, int sm_count, Geometry* g) {
    const int L = lanes;
    if (L < 1 || L > kMaxLanes) return "lane count out of range";
-   // records per thread: 8 (measured faster than 16 on GB300: more resident
-   // warps hide the dispatch latency); PPI_GPU_RECORDS_PER_THREAD=16 selects
-   // 16 where the lane == tile-position path allows it
-   const char* env = std::getenv("PPI_GPU_RECORDS_PER_THREAD");
-   const bool allow16 = env && std::atoi(env) == 16;
-   int R = 8, P;
-   if (strategy == PPI_STRATEGY_PDP && allow16 && L % (32 * 16) == 0 && L / 16 <= 128) {
-      R = 16;
-      P = L / 16;
-   } else if (strategy == PPI_STRATEGY_PDP && L % (32 * 8) == 0 && L / 8 <= 128) {
-      P = L / 8;
+   // records per thread: kR (8 measured faster than 16 on GB300: more
+   // resident warps hide the dispatch latency)
+   const int R = kR;
+   int P;
+   if (strategy == PPI_STRATEGY_PDP && L % (32 * R) == 0 && L / R <= 128) {
+      P = L / R;   // lane == tile position: register accumulation
    } else {
-      const int need = (strategy == PPI_STRATEGY_DP) ? L : std::min(nlin, 128 * 8);
-      P = std::min(128, std::max(32, ((need + 7) / 8 + 31) / 32 * 32));
+      const int need = (strategy == PPI_STRATEGY_DP) ? L : std::min(nlin, 128 * R);
+      P = std::min(128, std::max(32, ((need + R - 1) / R + 31) / 32 * 32));
    }
    if (strategy == PPI_STRATEGY_DP && L > P * R)
       return "DP lanes above 1024 records per group are not supported";
@@ -92,11 +102,12 @@ const char* plan_geometry(int strategy, int lanes, int math, int nlin, int ncol,
    }
    if (smem > 200 * 1024) return "dataset has too many columns for one shared-memory tile";
    int per_sm = 0;
-   if (evaluate_occupancy(math, R, P, smem, &per_sm) != cudaSuccess || per_sm < 1)
+   if (evaluate_occupancy(math, opset, P, smem, &per_sm) != cudaSuccess || per_sm < 1)
       return "evaluator does not fit on an SM";
    g->lanes = L;
    g->block = P;
    g->R = R;
+   g->opset = opset;
    g->smem = smem;
    g->grid = std::max(1, std::min(n_max, per_sm * sm_count));
    return nullptr;

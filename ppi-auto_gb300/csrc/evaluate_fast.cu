@@ -4,13 +4,13 @@
 
 namespace ppi {
 template struct ev::Launch<kMathFast>;
-cudaError_t launch_evaluate_fast(int R, const EvalArgs& a, int block, int grid, size_t smem, cudaStream_t s) {
-   return ev::Launch<kMathFast>::evaluate(R, a, block, grid, smem, s);
+cudaError_t launch_evaluate_fast(int opset, const EvalArgs& a, int block, int grid, size_t smem, cudaStream_t s) {
+   return ev::Launch<kMathFast>::evaluate(opset, a, block, grid, smem, s);
 }
-cudaError_t launch_predict_fast(int R, const PredictArgs& a, int block, int grid, size_t smem, cudaStream_t s) {
-   return ev::Launch<kMathFast>::predict(R, a, block, grid, smem, s);
+cudaError_t launch_predict_fast(int opset, const PredictArgs& a, int block, int grid, size_t smem, cudaStream_t s) {
+   return ev::Launch<kMathFast>::predict(opset, a, block, grid, smem, s);
 }
-cudaError_t evaluate_occupancy_fast(int R, int block, size_t smem, int* per_sm) {
-   return ev::Launch<kMathFast>::occupancy(R, block, smem, per_sm);
+cudaError_t evaluate_occupancy_fast(int opset, int block, size_t smem, int* per_sm) {
+   return ev::Launch<kMathFast>::occupancy(opset, block, smem, per_sm);
 }
 }  // namespace ppi

@@ -55,91 +55,48 @@ __device__ __forceinline__ void store_row(float* p, int P, const float (&x)[R]) 
 }
 
 // ---- bytecode path -------------------------------------------------------------
-// `mine` points at this thread's first quad of row 0; row k is at mine + k*T.
-template <int MATH, int R>
+// Opcode sets of the bytecode path.  FULL: every opcode.  ARITH: the
+// arithmetic grammars' opcodes (+ - * / sin cos exp log sqrt ^2 abs neg); a
+// program using anything else never reaches an ARITH kernel (the host picks
+// the set from the symbol table).
+#define PPI_FULL_UNARY(X) X(PPI_OP_NOT) X(PPI_OP_ABS) X(PPI_OP_POW2) X(PPI_OP_POW3) X(PPI_OP_POW4) \
+   X(PPI_OP_POW5) X(PPI_OP_NEG) X(PPI_OP_ROUND) X(PPI_OP_CEIL) X(PPI_OP_FLOOR) X(PPI_OP_EXP)      \
+   X(PPI_OP_EXP10) X(PPI_OP_EXP2) X(PPI_OP_SIN) X(PPI_OP_COS) X(PPI_OP_STEP) X(PPI_OP_SIGN)       \
+   X(PPI_OP_LOGISTIC) X(PPI_OP_GAMMA) X(PPI_OP_GAUSS) X(PPI_OP_SQRT) X(PPI_OP_LOG)               \
+   X(PPI_OP_LOG10) X(PPI_OP_LOG2) X(PPI_OP_TAN)
+#define PPI_FULL_BINARY(X) X(PPI_OP_AND) X(PPI_OP_OR) X(PPI_OP_XOR) X(PPI_OP_GREATER)           \
+   X(PPI_OP_GREATEREQUAL) X(PPI_OP_LESS) X(PPI_OP_LESSEQUAL) X(PPI_OP_EQUAL) X(PPI_OP_NOTEQUAL) \
+   X(PPI_OP_ADD) X(PPI_OP_SUB) X(PPI_OP_MULT) X(PPI_OP_MEAN) X(PPI_OP_MAX) X(PPI_OP_MIN)        \
+   X(PPI_OP_MOD) X(PPI_OP_POW) X(PPI_OP_DIV)
+#define PPI_ARITH_UNARY(X) X(PPI_OP_ABS) X(PPI_OP_POW2) X(PPI_OP_NEG) X(PPI_OP_EXP) X(PPI_OP_SIN) \
+   X(PPI_OP_COS) X(PPI_OP_SQRT) X(PPI_OP_LOG)
+#define PPI_ARITH_BINARY(X) X(PPI_OP_ADD) X(PPI_OP_SUB) X(PPI_OP_MULT) X(PPI_OP_DIV)
+
+#define PPI_RUN_FAST_NAME run_fast_full
+#define PPI_UNARY_LIST PPI_FULL_UNARY
+#define PPI_BINARY_LIST PPI_FULL_BINARY
+#define PPI_WITH_ITE 1
+#include "run_fast.inc"
+#undef PPI_RUN_FAST_NAME
+#undef PPI_UNARY_LIST
+#undef PPI_BINARY_LIST
+#undef PPI_WITH_ITE
+
+#define PPI_RUN_FAST_NAME run_fast_arith
+#define PPI_UNARY_LIST PPI_ARITH_UNARY
+#define PPI_BINARY_LIST PPI_ARITH_BINARY
+#define PPI_WITH_ITE 0
+#include "run_fast.inc"
+#undef PPI_RUN_FAST_NAME
+#undef PPI_UNARY_LIST
+#undef PPI_BINARY_LIST
+#undef PPI_WITH_ITE
+
+template <int MATH, int R, int OPSET>
 __device__ __forceinline__ void run_fast(const uint2* __restrict__ code, float* mine, int T, int P,
                                          float (&acc)[R], int prot) {
-   int pc = 0;
-   uint2 ins = code[0];
-   for (;;) {
-      const uint2 nxt = code[pc + 1];
-      switch (ins.x) {
-      case M_END: return;
-      case M_LD_ROW: load_row(mine + (size_t)ins.y * T, P, acc); break;
-      case M_LD_C: {
-         const float k = __uint_as_float(ins.y);
-#pragma unroll
-         for (int r = 0; r < R; ++r) acc[r] = k;
-         break;
-      }
-      case M_PUSH: store_row(mine + (size_t)ins.y * T, P, acc); break;
-
-#define PPI_UN_CASE(OP)                                                            \
-      case M_UN + (OP - PPI_OP_NOT):                                               \
-         _Pragma("unroll") for (int r = 0; r < R; ++r) acc[r] = unop<OP, MATH>(acc[r], prot); \
-         break;
-      PPI_UN_CASE(PPI_OP_NOT) PPI_UN_CASE(PPI_OP_ABS) PPI_UN_CASE(PPI_OP_POW2)
-      PPI_UN_CASE(PPI_OP_POW3) PPI_UN_CASE(PPI_OP_POW4) PPI_UN_CASE(PPI_OP_POW5)
-      PPI_UN_CASE(PPI_OP_NEG) PPI_UN_CASE(PPI_OP_ROUND) PPI_UN_CASE(PPI_OP_CEIL)
-      PPI_UN_CASE(PPI_OP_FLOOR) PPI_UN_CASE(PPI_OP_EXP) PPI_UN_CASE(PPI_OP_EXP10)
-      PPI_UN_CASE(PPI_OP_EXP2) PPI_UN_CASE(PPI_OP_SIN) PPI_UN_CASE(PPI_OP_COS)
-      PPI_UN_CASE(PPI_OP_STEP) PPI_UN_CASE(PPI_OP_SIGN) PPI_UN_CASE(PPI_OP_LOGISTIC)
-      PPI_UN_CASE(PPI_OP_GAMMA) PPI_UN_CASE(PPI_OP_GAUSS) PPI_UN_CASE(PPI_OP_SQRT)
-      PPI_UN_CASE(PPI_OP_LOG) PPI_UN_CASE(PPI_OP_LOG10) PPI_UN_CASE(PPI_OP_LOG2)
-      PPI_UN_CASE(PPI_OP_TAN)
-#undef PPI_UN_CASE
-
-#define PPI_BIN_CASES(OP)                                                          \
-      case M_BR_L + (OP - PPI_OP_AND): {                                           \
-         float x[R];                                                              \
-         load_row(mine + (size_t)ins.y * T, P, x);                                    \
-         _Pragma("unroll") for (int r = 0; r < R; ++r) acc[r] = binop<OP, MATH>(acc[r], x[r], prot); \
-         break;                                                                    \
-      }                                                                            \
-      case M_BR_R + (OP - PPI_OP_AND): {                                           \
-         float x[R];                                                              \
-         load_row(mine + (size_t)ins.y * T, P, x);                                    \
-         _Pragma("unroll") for (int r = 0; r < R; ++r) acc[r] = binop<OP, MATH>(x[r], acc[r], prot); \
-         break;                                                                    \
-      }                                                                            \
-      case M_BC_L + (OP - PPI_OP_AND): {                                           \
-         const float k = __uint_as_float(ins.y);                                   \
-         _Pragma("unroll") for (int r = 0; r < R; ++r) acc[r] = binop<OP, MATH>(acc[r], k, prot); \
-         break;                                                                    \
-      }                                                                            \
-      case M_BC_R + (OP - PPI_OP_AND): {                                           \
-         const float k = __uint_as_float(ins.y);                                   \
-         _Pragma("unroll") for (int r = 0; r < R; ++r) acc[r] = binop<OP, MATH>(k, acc[r], prot); \
-         break;                                                                    \
-      }
-      PPI_BIN_CASES(PPI_OP_AND) PPI_BIN_CASES(PPI_OP_OR) PPI_BIN_CASES(PPI_OP_XOR)
-      PPI_BIN_CASES(PPI_OP_GREATER) PPI_BIN_CASES(PPI_OP_GREATEREQUAL)
-      PPI_BIN_CASES(PPI_OP_LESS) PPI_BIN_CASES(PPI_OP_LESSEQUAL) PPI_BIN_CASES(PPI_OP_EQUAL)
-      PPI_BIN_CASES(PPI_OP_NOTEQUAL) PPI_BIN_CASES(PPI_OP_ADD) PPI_BIN_CASES(PPI_OP_SUB)
-      PPI_BIN_CASES(PPI_OP_MULT) PPI_BIN_CASES(PPI_OP_MEAN) PPI_BIN_CASES(PPI_OP_MAX)
-      PPI_BIN_CASES(PPI_OP_MIN) PPI_BIN_CASES(PPI_OP_MOD) PPI_BIN_CASES(PPI_OP_POW)
-      PPI_BIN_CASES(PPI_OP_DIV)
-#undef PPI_BIN_CASES
-
-#define PPI_ITE_CASE(PERM)                                                            \
-      case M_ITE + PERM: {                                                            \
-         float ra[R], rb[R];                                                     \
-         load_row(mine + (size_t)(ins.y & 0xFFFFu) * T, P, ra);                       \
-         load_row(mine + (size_t)(ins.y >> 16) * T, P, rb);                           \
-         _Pragma("unroll") for (int r = 0; r < R; ++r) {                          \
-            const float v3[3] = {acc[r], ra[r], rb[r]};                            \
-            acc[r] = truthy(v3[ite_role(PERM, 0)]) ? v3[ite_role(PERM, 1)] : v3[ite_role(PERM, 2)]; \
-         }                                                                         \
-         break;                                                                    \
-      }
-      PPI_ITE_CASE(0) PPI_ITE_CASE(1) PPI_ITE_CASE(2) PPI_ITE_CASE(3) PPI_ITE_CASE(4)
-      PPI_ITE_CASE(5)
-#undef PPI_ITE_CASE
-      default: __builtin_unreachable();
-      }
-      ins = nxt;
-      ++pc;
-   }
+   if constexpr (OPSET == kOpsetArith) run_fast_arith<MATH, R>(code, mine, T, P, acc, prot);
+   else run_fast_full<MATH, R>(code, mine, T, P, acc, prot);
 }
 
 // ---- generic stack interpreter ----------------------------------------------
@@ -250,7 +207,7 @@ __device__ __forceinline__ void local_tree(float* pe, int L, int reduce_max, int
    }
 }
 
-template <int MATH, int R>
+template <int MATH, int R, int OPSET>
 __global__ void __launch_bounds__(128, 4) eval_kernel(const EvalArgs a) {
    extern __shared__ __align__(16) unsigned char smem_raw[];
    __shared__ int s_prog;
@@ -305,7 +262,7 @@ __global__ void __launch_bounds__(128, 4) eval_kernel(const EvalArgs a) {
             __syncthreads();
             float v[R];
             if (m.x == kKindFast) {
-               run_fast<MATH, R>(s_code, s_tile + tid * 4, T, P, v, a.prot);
+               run_fast<MATH, R, OPSET>(s_code, s_tile + tid * 4, T, P, v, a.prot);
             } else {
                float tmp[R];
                run_generic<MATH, R>(s_code, s_tile, T, P, tid, tmp, a.prot);
@@ -409,7 +366,7 @@ __global__ void __launch_bounds__(128, 4) eval_kernel(const EvalArgs a) {
 }
 
 // Per-record predictions of program 0 (ppp prediction mode).
-template <int MATH, int R>
+template <int MATH, int R, int OPSET>
 __global__ void __launch_bounds__(128, 4) predict_kernel(const PredictArgs a) {
    extern __shared__ __align__(16) unsigned char smem_raw[];
    const int P = blockDim.x, tid = threadIdx.x, T = P * R;
@@ -428,7 +385,7 @@ __global__ void __launch_bounds__(128, 4) predict_kernel(const PredictArgs a) {
       __syncthreads();
       float v[R];
       if (m.x == kKindFast) {
-         run_fast<MATH, R>(s_code, s_tile + tid * 4, T, P, v, a.prot);
+         run_fast<MATH, R, OPSET>(s_code, s_tile + tid * 4, T, P, v, a.prot);
       } else if (m.x == kKindGeneric) {
          float tmp[R];
          run_generic<MATH, R>(s_code, s_tile, T, P, tid, tmp, a.prot);
@@ -447,35 +404,36 @@ __global__ void __launch_bounds__(128, 4) predict_kernel(const PredictArgs a) {
 }
 
 
-template <int MATH, int R>
+template <int MATH, int OPSET>
 cudaError_t configure_t() {
-   cudaError_t e = cudaFuncSetAttribute(eval_kernel<MATH, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+   cudaError_t e = cudaFuncSetAttribute(eval_kernel<MATH, kR, OPSET>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
    if (e != cudaSuccess) return e;
-   return cudaFuncSetAttribute(predict_kernel<MATH, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+   return cudaFuncSetAttribute(predict_kernel<MATH, kR, OPSET>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
 }
 
-// Per-math entry points, instantiated in evaluate_<math>.cu.
+// Per-math entry points, instantiated in evaluate_<math>.cu (R = kR records
+// per thread; opset 0 = FULL, 1 = ARITH).
 template <int MATH>
 struct Launch {
-   static cudaError_t evaluate(int R, const EvalArgs& a, int block, int grid, size_t smem, cudaStream_t s) {
-      cudaError_t e = R == 16 ? configure_t<MATH, 16>() : configure_t<MATH, 8>();
+   static cudaError_t evaluate(int opset, const EvalArgs& a, int block, int grid, size_t smem, cudaStream_t s) {
+      cudaError_t e = opset ? configure_t<MATH, kOpsetArith>() : configure_t<MATH, kOpsetFull>();
       if (e != cudaSuccess) return e;
-      if (R == 16) eval_kernel<MATH, 16><<<grid, block, smem, s>>>(a);
-      else eval_kernel<MATH, 8><<<grid, block, smem, s>>>(a);
+      if (opset) eval_kernel<MATH, kR, kOpsetArith><<<grid, block, smem, s>>>(a);
+      else eval_kernel<MATH, kR, kOpsetFull><<<grid, block, smem, s>>>(a);
       return cudaGetLastError();
    }
-   static cudaError_t predict(int R, const PredictArgs& a, int block, int grid, size_t smem, cudaStream_t s) {
-      cudaError_t e = R == 16 ? configure_t<MATH, 16>() : configure_t<MATH, 8>();
+   static cudaError_t predict(int opset, const PredictArgs& a, int block, int grid, size_t smem, cudaStream_t s) {
+      cudaError_t e = opset ? configure_t<MATH, kOpsetArith>() : configure_t<MATH, kOpsetFull>();
       if (e != cudaSuccess) return e;
-      if (R == 16) predict_kernel<MATH, 16><<<grid, block, smem, s>>>(a);
-      else predict_kernel<MATH, 8><<<grid, block, smem, s>>>(a);
+      if (opset) predict_kernel<MATH, kR, kOpsetArith><<<grid, block, smem, s>>>(a);
+      else predict_kernel<MATH, kR, kOpsetFull><<<grid, block, smem, s>>>(a);
       return cudaGetLastError();
    }
-   static cudaError_t occupancy(int R, int block, size_t smem, int* per_sm) {
-      cudaError_t e = R == 16 ? configure_t<MATH, 16>() : configure_t<MATH, 8>();
+   static cudaError_t occupancy(int opset, int block, size_t smem, int* per_sm) {
+      cudaError_t e = opset ? configure_t<MATH, kOpsetArith>() : configure_t<MATH, kOpsetFull>();
       if (e != cudaSuccess) return e;
-      if (R == 16) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, eval_kernel<MATH, 16>, block, smem);
-      return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, eval_kernel<MATH, 8>, block, smem);
+      if (opset) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, eval_kernel<MATH, kR, kOpsetArith>, block, smem);
+      return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, eval_kernel<MATH, kR, kOpsetFull>, block, smem);
    }
 };
 

@@ -4,13 +4,13 @@
 
 namespace ppi {
 template struct ev::Launch<kMathNative>;
-cudaError_t launch_evaluate_native(int R, const EvalArgs& a, int block, int grid, size_t smem, cudaStream_t s) {
-   return ev::Launch<kMathNative>::evaluate(R, a, block, grid, smem, s);
+cudaError_t launch_evaluate_native(int opset, const EvalArgs& a, int block, int grid, size_t smem, cudaStream_t s) {
+   return ev::Launch<kMathNative>::evaluate(opset, a, block, grid, smem, s);
 }
-cudaError_t launch_predict_native(int R, const PredictArgs& a, int block, int grid, size_t smem, cudaStream_t s) {
-   return ev::Launch<kMathNative>::predict(R, a, block, grid, smem, s);
+cudaError_t launch_predict_native(int opset, const PredictArgs& a, int block, int grid, size_t smem, cudaStream_t s) {
+   return ev::Launch<kMathNative>::predict(opset, a, block, grid, smem, s);
 }
-cudaError_t evaluate_occupancy_native(int R, int block, size_t smem, int* per_sm) {
-   return ev::Launch<kMathNative>::occupancy(R, block, smem, per_sm);
+cudaError_t evaluate_occupancy_native(int opset, int block, size_t smem, int* per_sm) {
+   return ev::Launch<kMathNative>::occupancy(opset, block, smem, per_sm);
 }
 }  // namespace ppi

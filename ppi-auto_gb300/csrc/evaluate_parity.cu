@@ -4,13 +4,13 @@
 
 namespace ppi {
 template struct ev::Launch<kMathParity>;
-cudaError_t launch_evaluate_parity(int R, const EvalArgs& a, int block, int grid, size_t smem, cudaStream_t s) {
-   return ev::Launch<kMathParity>::evaluate(R, a, block, grid, smem, s);
+cudaError_t launch_evaluate_parity(int opset, const EvalArgs& a, int block, int grid, size_t smem, cudaStream_t s) {
+   return ev::Launch<kMathParity>::evaluate(opset, a, block, grid, smem, s);
 }
-cudaError_t launch_predict_parity(int R, const PredictArgs& a, int block, int grid, size_t smem, cudaStream_t s) {
-   return ev::Launch<kMathParity>::predict(R, a, block, grid, smem, s);
+cudaError_t launch_predict_parity(int opset, const PredictArgs& a, int block, int grid, size_t smem, cudaStream_t s) {
+   return ev::Launch<kMathParity>::predict(opset, a, block, grid, smem, s);
 }
-cudaError_t evaluate_occupancy_parity(int R, int block, size_t smem, int* per_sm) {
-   return ev::Launch<kMathParity>::occupancy(R, block, smem, per_sm);
+cudaError_t evaluate_occupancy_parity(int opset, int block, size_t smem, int* per_sm) {
+   return ev::Launch<kMathParity>::occupancy(opset, block, smem, per_sm);
 }
 }  // namespace ppi

@@ -127,7 +127,8 @@ extern "C" ppi_status ppi_gpu_evaluate_noalloc(const ppi_gpu_config* c, const fl
       return PPI_ERR_CUDA;
    Geometry g;
    const int L = resolve_lanes(c->strategy, c->lanes, nlin, sm_count);
-   if (plan_geometry(c->strategy, L, c->math, nlin, ncol, code_stride, n, sm_count, &g))
+   if (plan_geometry(c->strategy, L, c->math, opset_for(c->symbols, c->n_symbols), nlin, ncol,
+                     code_stride, n, sm_count, &g))
       return PPI_ERR_UNSUPPORTED;
 
    unsigned char* base = nullptr;
@@ -167,6 +168,6 @@ extern "C" ppi_status ppi_gpu_evaluate_noalloc(const ppi_gpu_config* c, const fl
    e.cost = cost; e.cost_n = c->cost_n; e.strategy = c->strategy; e.lanes = g.lanes; e.fitness = d_fitness;
    e.best_key = key; e.counters = counters; e.best_index = d_best_index; e.status = status;
    if (launch_translate(c->math, t, s) != cudaSuccess) return PPI_ERR_CUDA;
-   if (launch_evaluate(c->math, g.R, e, g.block, g.grid, g.smem, s) != cudaSuccess) return PPI_ERR_CUDA;
+   if (launch_evaluate(c->math, g.opset, e, g.block, g.grid, g.smem, s) != cudaSuccess) return PPI_ERR_CUDA;
    return PPI_OK;
 }

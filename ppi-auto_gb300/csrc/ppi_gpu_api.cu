@@ -33,6 +33,7 @@ struct ppi_gpu {
    int nlin = 0, ncol = 0, ld = 0;
    bool have_data = false;
    int lanes = 1;
+   int opset = kOpsetFull;
    Geometry geo;
    // per-generation buffers (capacity population_size)
    int32_t* d_ph = nullptr;
@@ -106,8 +107,8 @@ void free_all(ppi_gpu* h) {
 // Evaluator geometry for the current dataset and lane count.
 ppi_status plan(ppi_gpu* h) {
    Geometry g;
-   const char* why = plan_geometry(h->cfg.strategy, h->lanes, h->cfg.math, h->nlin, h->ncol,
-                                   h->code_stride, h->cfg.population_size, h->sm_count, &g);
+   const char* why = plan_geometry(h->cfg.strategy, h->lanes, h->cfg.math, h->opset, h->nlin,
+                                   h->ncol, h->code_stride, h->cfg.population_size, h->sm_count, &g);
    if (why) return fail(h, PPI_ERR_UNSUPPORTED, why);
    h->geo = g;
    return PPI_OK;
@@ -141,7 +142,7 @@ ppi_status enqueue(ppi_gpu* h, const int32_t* d_ph, const float* d_eph, const in
    PPI_CUDA(h, cudaEventRecord(h->ev0, s));
    PPI_CUDA(h, launch_translate(h->cfg.math, t, s));
    PPI_CUDA(h, cudaEventRecord(h->evm, s));
-   PPI_CUDA(h, launch_evaluate(h->cfg.math, h->geo.R, e, h->geo.block, std::min(h->geo.grid, n),
+   PPI_CUDA(h, launch_evaluate(h->cfg.math, h->geo.opset, e, h->geo.block, std::min(h->geo.grid, n),
                                h->geo.smem, s));
    PPI_CUDA(h, cudaEventRecord(h->ev1, s));
    h->last_launches = 2;
@@ -195,6 +196,7 @@ ppi_status ppi_gpu_create(const ppi_gpu_config* c, ppi_gpu** out) {
       std::memcpy(&bits, &c->symbols[i].value, 4);
       lut[(size_t)(c->symbols[i].symbol - mn)] = make_int2(c->symbols[i].op, bits);
    }
+   h->opset = opset_for(c->symbols, c->n_symbols);
    h->lut_min = mn;
    h->lut_len = c->n_symbols > 0 ? mx - mn + 1 : 0;
    const size_t pop = (size_t)c->population_size, ms = (size_t)c->max_size;
@@ -362,7 +364,7 @@ ppi_status ppi_gpu_predict(ppi_gpu* h, const int32_t* ph, const float* eph, int3
    const int grid = std::max(1, std::min(tiles, 4 * h->sm_count));
    PPI_CUDA(h, cudaEventRecord(h->ev0, h->stream));
    PPI_CUDA(h, launch_translate(h->cfg.math, t, h->stream));
-   PPI_CUDA(h, launch_predict(h->cfg.math, R, p, P, grid, smem, h->stream));
+   PPI_CUDA(h, launch_predict(h->cfg.math, h->opset, p, P, grid, smem, h->stream));
    PPI_CUDA(h, cudaEventRecord(h->ev1, h->stream));
    PPI_CUDA(h, cudaMemcpyAsync(out, h->d_pred, (size_t)h->nlin * 4, cudaMemcpyDeviceToHost, h->stream));
    PPI_CUDA(h, cudaStreamSynchronize(h->stream));

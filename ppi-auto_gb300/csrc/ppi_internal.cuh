@@ -26,6 +26,9 @@ constexpr int kGenericStack = 128;
 // Column stride of the device dataset is a multiple of this.
 constexpr int kColumnPad = 1024;
 
+// Opcode sets of the evaluator's bytecode path (evaluate_impl.cuh).
+enum : int { kOpsetFull = 0, kOpsetArith = 1 };
+
 // Program kinds written by the translator.
 enum : int { kKindInvalid = 0, kKindFast = 1, kKindGeneric = 2, kKindUnsupported = 3 };
 
@@ -287,21 +290,23 @@ struct PredictArgs {
 // Evaluator launch geometry: lanes, block size P, records per thread R,
 // dynamic shared memory and a one-wave persistent grid.
 struct Geometry {
-   int lanes = 1, block = 128, R = 8, grid = 1;
+   int lanes = 1, block = 128, R = 8, grid = 1, opset = kOpsetFull;
    size_t smem = 0;
 };
+// kOpsetArith when every op of the symbol table is in the ARITH set.
+int opset_for(const ppi_symbol_entry* symbols, int n);
 int resolve_lanes(int strategy, int lanes, int nlin, int sm_count);
 // Returns nullptr on success, else why the configuration is unsupported.
-const char* plan_geometry(int strategy, int lanes, int math, int nlin, int ncol, int code_stride,
-                          int n_max, int sm_count, Geometry* g);
+const char* plan_geometry(int strategy, int lanes, int math, int opset, int nlin, int ncol,
+                          int code_stride, int n_max, int sm_count, Geometry* g);
 
 // Kernel launchers (evaluate.cu / translate.cu).
 cudaError_t launch_translate(int math, const TranslateArgs& a, cudaStream_t s);
-cudaError_t launch_evaluate(int math, int R, const EvalArgs& a, int block, int grid, size_t smem,
+cudaError_t launch_evaluate(int math, int opset, const EvalArgs& a, int block, int grid, size_t smem,
                             cudaStream_t s);
-cudaError_t launch_predict(int math, int R, const PredictArgs& a, int block, int grid, size_t smem,
+cudaError_t launch_predict(int math, int opset, const PredictArgs& a, int block, int grid, size_t smem,
                            cudaStream_t s);
-cudaError_t evaluate_occupancy(int math, int R, int block, size_t smem, int* blocks_per_sm);
+cudaError_t evaluate_occupancy(int math, int opset, int block, size_t smem, int* blocks_per_sm);
 size_t evaluate_smem_bytes(int code_stride, int ncol, int block, int R, int lanes, bool aligned);
 
 }  // namespace ppi
