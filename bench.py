@@ -222,12 +222,14 @@ def run_ours(args):
     ev_s = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     ev_e = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     eval_ms = []
+    launches = 0
     for k in range(args.steps):
         flush.zero_()
         ev_s[k].record(stream)
         step()
         ev_e[k].record(stream)
         eval_ms.append(ev.last_stage_ms()[1])
+        launches += ev.last_launch_count()
     torch.cuda.synchronize(dev)
     if world > 1:
         torch.distributed.barrier()
@@ -283,7 +285,7 @@ def run_ours(args):
         "e2e": {"value": round(e2e, 3), "unit": UNIT,
                 "h2d_bytes_per_step": int(ph.nbytes + eph.nbytes + sz.nbytes),
                 "d2h_bytes_per_step": int(n * 4 + 4)},
-        "gpu_launches": 2 * args.steps,
+        "gpu_launches": launches,
         "roofline": {"bound": "fp32_issue", "achieved": round(achieved, 2),
                      "peak": round(peak, 1), "unit": "Gop/s", "frac": round(achieved / peak, 4),
                      "peak_source": "SMs x 128 FP32 lanes x sm_max_mhz (MEASURED_PEAKS.json)",

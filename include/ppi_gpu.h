@@ -202,6 +202,51 @@ int32_t ppi_gpu_lanes(const ppi_gpu* h);
 /* Number of kernel launches the last evaluate / predict / decode call made. */
 int32_t ppi_gpu_last_launch_count(const ppi_gpu* h);
 
+/* ---- batches: many populations in one launch ------------------------------
+ * No single reference function: this evaluates what several acc_interpret
+ * calls would (one per population, e.g. one per island or per independent
+ * run) in one persistent launch.  Each population keeps its own dataset,
+ * strategy, lanes, error function, REDUCEMAX and PROTECTED settings, and its
+ * fitness values are bit-identical to ppi_gpu_evaluate on that population
+ * alone. */
+typedef struct {
+   const float* rows;         /* row-major nlin x ncol, target in the last column (copied) */
+   int32_t nlin, ncol;
+   int32_t n;                 /* programs in this population                         */
+   int32_t strategy, lanes, error_fn, reduce_max, protected_fns;
+   const float* cost;         /* PPI_EF_COST only (copied)                           */
+   int32_t cost_n;
+} ppi_batch_population;
+
+#define PPI_BATCH_GRAPH 1     /* capture the step into a CUDA graph and replay it   */
+#define PPI_BATCH_AUTOTUNE 2  /* on the first call, time each block shape, keep the fastest */
+
+typedef struct ppi_batch ppi_batch;
+
+/* config: max_size (row stride), math, symbols and device are used; the other
+ * fields are per population. */
+ppi_status ppi_batch_create(const ppi_gpu_config* config, int32_t n_pops,
+                            const ppi_batch_population* pops, ppi_batch** out);
+ppi_status ppi_batch_destroy(ppi_batch* b);
+const char* ppi_batch_last_error(const ppi_batch* b);
+/* alpha (the complexity penalty) of each population; 0 until set. */
+ppi_status ppi_batch_set_alpha(ppi_batch* b, const float* alpha);
+/* All populations' programs concatenated in population order (rows of
+ * max_size); fitness likewise; best_index: one per population. */
+ppi_status ppi_batch_evaluate(ppi_batch* b, const int32_t* phenotype, const float* ephemeral,
+                              const int32_t* size, float* fitness, int32_t* best_index,
+                              int32_t flags);
+/* Device-resident form on `stream`; PPI_BATCH_GRAPH needs a non-NULL stream. */
+ppi_status ppi_batch_evaluate_device(ppi_batch* b, const int32_t* d_phenotype,
+                                     const float* d_ephemeral, const int32_t* d_size,
+                                     float* d_fitness, int32_t* d_best_index, void* stream,
+                                     int32_t flags);
+/* Device time of the last step (waits for it). */
+ppi_status ppi_batch_last_kernel_ms(ppi_batch* b, float* ms);
+/* Block size and grid in use; tune_ms (may be NULL) receives the autotuner's
+ * timings of the 64- and 128-thread shapes (-1: shape does not fit). */
+ppi_status ppi_batch_shape(const ppi_batch* b, int32_t* block, int32_t* grid, float* tune_ms);
+
 /* No counterpart in the reference.  One generation evaluated without
  * allocating any memory, for callers that cannot allocate where they evaluate:
  * an application whose device memory another allocator has already reserved,

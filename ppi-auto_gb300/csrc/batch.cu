@@ -1,0 +1,495 @@
+// batch.cu -- many populations evaluated by one persistent launch.
+//
+// A GE run with several islands, or several independent runs, has
+// populations of very different sizes, program lengths and datasets.  One
+// plain evaluation per population leaves most of the GPU idle on the small
+// ones and pays a tail on every launch.  Here all programs of all populations
+// form one work queue, ordered by cost (size x records, largest first, via
+// 64 power-of-two buckets counted by the translator), and one persistent grid
+// drains it.  Each population keeps its own strategy, lane count, error
+// function and accumulation order, so every fitness is bit-identical to the
+// plain evaluation of that population.
+//
+// Each CTA stages only the columns its current program reads, so the tile's
+// shared memory follows the program, not the widest dataset of the batch.
+// The main pass runs every program whose tile fits its row budget (the most
+// rows at full occupancy, or what the row histogram of an earlier evaluation
+// asks for); the wide pass runs the rest with a larger tile.
+// Per generation the device work is: memsets, the translator, the order
+// scan, the order scatter and the two passes.  With PPI_BATCH_GRAPH it is
+// captured once into a CUDA graph and replayed.  PPI_BATCH_AUTOTUNE sizes
+// the main pass's rows from a first evaluation's row histogram, then times
+// both block shapes (64 or 128 threads per CTA) and keeps the faster; it
+// changes speed only, never a result.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "ppi_internal.cuh"
+
+namespace ppi {
+namespace {
+
+// Cost buckets: [0, 64) programs of the main pass, [64, 128) of the wide pass.
+constexpr int kBuckets = 128;
+
+// Exclusive offsets of the cost buckets (one thread): the main pass's
+// programs first, each pass largest bucket first; *n_main = main-pass items.
+__global__ void batch_scan_kernel(const unsigned* count, unsigned* cursor, unsigned* n_main) {
+   if (blockIdx.x == 0 && threadIdx.x == 0) {
+      unsigned off = 0;
+      for (int b = 63; b >= 0; --b) {
+         cursor[b] = off;
+         off += count[b];
+      }
+      *n_main = off;
+      for (int b = 127; b >= 64; --b) {
+         cursor[b] = off;
+         off += count[b];
+      }
+   }
+}
+
+__global__ void batch_scatter_kernel(const unsigned char* bucket_of, unsigned* cursor, int* order,
+                                     int total) {
+   const int i = blockIdx.x * blockDim.x + threadIdx.x;
+   if (i >= total) return;
+   const unsigned pos = atomicAdd(&cursor[bucket_of[i]], 1u);
+   order[pos] = i;
+}
+
+}  // namespace
+
+cudaError_t launch_batch_order(const unsigned* bucket_count, unsigned* cursor,
+                               const unsigned char* bucket_of, int* order, int total,
+                               unsigned* n_main, cudaStream_t s) {
+   batch_scan_kernel<<<1, 32, 0, s>>>(bucket_count, cursor, n_main);
+   cudaError_t e = cudaGetLastError();
+   if (e != cudaSuccess) return e;
+   batch_scatter_kernel<<<std::max(1, (total + 255) / 256), 256, 0, s>>>(bucket_of, cursor, order, total);
+   return cudaGetLastError();
+}
+
+}  // namespace ppi
+
+using namespace ppi;
+
+// Launch shape of the two passes.
+struct BatchGeo {
+   int block = 128;
+   int rows = 1, grid = 1;
+   size_t smem = 0;
+   int rows_wide = 1, grid_wide = 1;
+   size_t smem_wide = 0;
+   bool wide = false;
+};
+
+struct ppi_batch {
+   int device = 0, sm_count = 0, math = 0, max_size = 0, opset = kOpsetFull;
+   int n_pops = 0, total = 0, code_stride = 0;
+   std::string err;
+   std::vector<PopDesc> host_pops;
+   std::vector<float*> datasets;
+   std::vector<float*> costs;
+   int2* d_lut = nullptr;
+   int lut_min = 0, lut_len = 0;
+   PopDesc* d_pops = nullptr;
+   int* d_pop_of = nullptr;
+   int* d_order = nullptr;
+   unsigned char* d_bucket_of = nullptr;
+   unsigned* d_bucket = nullptr;       // [0, kBuckets): counts, [kBuckets, 2 kBuckets): cursors
+   unsigned* d_n_main = nullptr;
+   unsigned long long* d_pop_key = nullptr;
+   unsigned* d_pop_done = nullptr;
+   int32_t* d_best = nullptr;
+   DevStats* d_stats = nullptr;
+   unsigned long long* d_key = nullptr;
+   int* d_status = nullptr;
+   int32_t* d_ph = nullptr;
+   float* d_eph = nullptr;
+   int32_t* d_size = nullptr;
+   float* d_fit = nullptr;
+   uint2* d_code = nullptr;
+   int2* d_meta = nullptr;
+   uint2* d_work = nullptr;
+   float* h_fit = nullptr;
+   int32_t* h_best = nullptr;
+   int* h_status = nullptr;
+   unsigned long long* h_rows = nullptr;
+   cudaStream_t stream = nullptr;
+   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+   // geometry
+   BatchGeo geo;
+   int max_ncol = 1, max_lanes_unaligned = 0;
+   bool tuned = false;
+   int tune_blocks[2] = {64, 128};
+   float tune_ms[2] = {0.0f, 0.0f};
+   // graph of one step, keyed by the buffers it was captured with
+   cudaGraphExec_t graph = nullptr;
+   const void* graph_key[6] = {};
+   cudaStream_t graph_stream = nullptr;
+   float last_ms = 0.0f;
+};
+
+namespace {
+
+ppi_status bfail(ppi_batch* b, ppi_status s, const std::string& m) {
+   if (b) b->err = m;
+   return s;
+}
+
+#define PPI_BCUDA(b, call)                                                                  \
+   do {                                                                                     \
+      cudaError_t e_ = (call);                                                              \
+      if (e_ != cudaSuccess)                                                                \
+         return bfail((b), e_ == cudaErrorMemoryAllocation ? PPI_ERR_OUT_OF_MEMORY : PPI_ERR_CUDA, \
+                      std::string(#call) + ": " + cudaGetErrorString(e_));                  \
+   } while (0)
+
+template <class T>
+cudaError_t balloc(T** p, size_t count) {
+   *p = nullptr;
+   return cudaMalloc(reinterpret_cast<void**>(p), std::max<size_t>(count, 1) * sizeof(T));
+}
+
+void bfree_all(ppi_batch* b) {
+   if (b->graph) cudaGraphExecDestroy(b->graph);
+   for (float* p : b->datasets) cudaFree(p);
+   for (float* p : b->costs) cudaFree(p);
+   cudaFree(b->d_lut); cudaFree(b->d_pops); cudaFree(b->d_pop_of); cudaFree(b->d_order);
+   cudaFree(b->d_bucket_of); cudaFree(b->d_bucket); cudaFree(b->d_pop_key); cudaFree(b->d_pop_done);
+   cudaFree(b->d_best); cudaFree(b->d_stats); cudaFree(b->d_key); cudaFree(b->d_status);
+   cudaFree(b->d_n_main); cudaFreeHost(b->h_rows);
+   cudaFree(b->d_ph); cudaFree(b->d_eph); cudaFree(b->d_size); cudaFree(b->d_fit);
+   cudaFree(b->d_code); cudaFree(b->d_meta); cudaFree(b->d_work);
+   cudaFreeHost(b->h_fit); cudaFreeHost(b->h_best); cudaFreeHost(b->h_status);
+   if (b->ev0) cudaEventDestroy(b->ev0);
+   if (b->ev1) cudaEventDestroy(b->ev1);
+   if (b->stream) cudaStreamDestroy(b->stream);
+}
+
+// Geometry for block size P: the main pass's rows (the most at the
+// occupancy of a one-row tile, or rows_hint when it asks for more) and the
+// wide pass's rows (every program of the widest dataset, up to 200 KB).
+ppi_status batch_geometry(ppi_batch* b, int P, int rows_hint, BatchGeo* g) {
+   for (const PopDesc& p : b->host_pops)
+      if (p.strategy == PPI_STRATEGY_DP && p.lanes > P * kR)
+         return bfail(b, PPI_ERR_UNSUPPORTED, "DP lanes larger than the tile");
+   constexpr size_t kSmemCap = 200 * 1024;
+   const size_t T = (size_t)P * kR;
+   // lane buffers of the populations that do not accumulate in registers
+   int lanes_extra = 0;
+   for (const PopDesc& p : b->host_pops)
+      if (!(p.strategy == PPI_STRATEGY_PDP && p.lanes == (int)T)) lanes_extra = std::max(lanes_extra, p.lanes);
+   auto smem_for = [&](int rows) {
+      return evaluate_smem_bytes(b->code_stride, rows, P, kR, lanes_extra, lanes_extra == 0);
+   };
+   const size_t fixed = smem_for(1) - T * 4;
+   if (fixed + T * 4 > kSmemCap) return bfail(b, PPI_ERR_UNSUPPORTED, "tile does not fit in shared memory");
+   const int rows_wide = (int)std::min<size_t>(max_program_rows(b->max_ncol), (kSmemCap - fixed) / (T * 4));
+   auto occupancy = [&](int rows) {
+      int per_sm = 0;
+      if (evaluate_batch_occupancy(b->math, b->opset, P, smem_for(rows), &per_sm) != cudaSuccess) return 0;
+      return per_sm;
+   };
+   const int top = occupancy(1);
+   if (top < 1) return bfail(b, PPI_ERR_UNSUPPORTED, "evaluator does not fit on an SM");
+   int rows = 1;
+   while (rows < rows_wide && occupancy(rows + 1) >= top) ++rows;
+   if (rows_hint > rows) rows = std::min(rows_hint, rows_wide);
+   g->block = P;
+   g->rows = rows;
+   g->smem = smem_for(rows);
+   g->grid = std::max(1, std::min(b->total, occupancy(rows) * b->sm_count));
+   g->rows_wide = rows_wide;
+   g->smem_wide = smem_for(rows_wide);
+   g->grid_wide = std::max(1, std::min(b->total, std::max(1, occupancy(rows_wide)) * b->sm_count));
+   g->wide = rows < rows_wide;
+   return PPI_OK;
+}
+
+ppi_status enqueue_step(ppi_batch* b, const int32_t* ph, const float* eph, const int32_t* size,
+                        float* fit, int32_t* best, cudaStream_t s, const BatchGeo& g) {
+   PPI_BCUDA(b, cudaMemsetAsync(b->d_stats, 0, sizeof(DevStats), s));
+   PPI_BCUDA(b, cudaMemsetAsync(b->d_bucket, 0, 2 * kBuckets * sizeof(unsigned), s));
+   PPI_BCUDA(b, cudaMemsetAsync(b->d_pop_key, 0xFF, b->n_pops * sizeof(unsigned long long), s));
+   PPI_BCUDA(b, cudaMemsetAsync(b->d_pop_done, 0, b->n_pops * sizeof(unsigned), s));
+   TranslateArgs t{};
+   t.phenotype = ph; t.ephemeral = eph; t.size = size; t.n = b->total; t.max_size = b->max_size;
+   t.ncol = 1; t.nlin = 1; t.lut = b->d_lut; t.lut_min = b->lut_min; t.lut_len = b->lut_len;
+   t.code = b->d_code; t.code_stride = b->code_stride; t.meta = b->d_meta; t.work = b->d_work;
+   t.best_key = b->d_key; t.stats = b->d_stats; t.status = b->d_status;
+   t.prot = -1; t.fold = 1;   // ncol, records and prot come from each program's population
+   t.rows_main = g.rows; t.rows_wide = g.rows_wide;
+   t.pop_of = b->d_pop_of; t.pops = b->d_pops; t.bucket_count = b->d_bucket; t.bucket_of = b->d_bucket_of;
+   PPI_BCUDA(b, launch_translate(b->math, t, s));
+   PPI_BCUDA(b, launch_batch_order(b->d_bucket, b->d_bucket + kBuckets, b->d_bucket_of, b->d_order,
+                                   b->total, b->d_n_main, s));
+   BatchArgs a{};
+   a.pops = b->d_pops; a.pop_of = b->d_pop_of; a.order = b->d_order; a.total = b->total;
+   a.code = b->d_code; a.code_stride = b->code_stride; a.meta = b->d_meta; a.size = size;
+   a.fitness = fit; a.pop_key = b->d_pop_key; a.pop_done = b->d_pop_done; a.best_index = best;
+   a.stats = b->d_stats; a.n_main = b->d_n_main; a.status = b->d_status;
+   a.rows = g.rows; a.wide_pass = 0;
+   PPI_BCUDA(b, launch_evaluate_batch(b->math, b->opset, a, g.block, g.grid, g.smem, s));
+   if (g.wide) {
+      a.rows = g.rows_wide; a.wide_pass = 1;
+      PPI_BCUDA(b, launch_evaluate_batch(b->math, b->opset, a, g.block, g.grid_wide, g.smem_wide, s));
+   }
+   return PPI_OK;
+}
+
+// Size the main pass's rows from a first evaluation's row histogram (all but
+// 1% of the work), then time both block shapes once on these inputs and keep
+// the faster.
+ppi_status autotune(ppi_batch* b, const int32_t* ph, const float* eph, const int32_t* size, float* fit,
+                    int32_t* best, cudaStream_t s) {
+   ppi_status st = enqueue_step(b, ph, eph, size, fit, best, s, b->geo);
+   if (st != PPI_OK) return st;
+   PPI_BCUDA(b, cudaMemcpyAsync(b->h_rows, b->d_stats->rows_work, kRowBins * sizeof(unsigned long long),
+                                cudaMemcpyDeviceToHost, s));
+   PPI_BCUDA(b, cudaStreamSynchronize(s));
+   const int hint = rows_for_histogram(b->h_rows, kRowBins, 0.01);
+   int best_i = -1;
+   BatchGeo geos[2];
+   for (int i = 0; i < 2; ++i) {
+      if (batch_geometry(b, b->tune_blocks[i], hint, &geos[i]) != PPI_OK) {
+         b->tune_ms[i] = -1.0f;
+         continue;
+      }
+      PPI_BCUDA(b, cudaEventRecord(b->ev0, s));
+      st = enqueue_step(b, ph, eph, size, fit, best, s, geos[i]);
+      if (st != PPI_OK) return st;
+      PPI_BCUDA(b, cudaEventRecord(b->ev1, s));
+      PPI_BCUDA(b, cudaEventSynchronize(b->ev1));
+      PPI_BCUDA(b, cudaEventElapsedTime(&b->tune_ms[i], b->ev0, b->ev1));
+      if (best_i < 0 || b->tune_ms[i] < b->tune_ms[best_i]) best_i = i;
+   }
+   if (best_i < 0) return bfail(b, PPI_ERR_UNSUPPORTED, "no block shape fits this batch");
+   b->geo = geos[best_i];
+   b->tuned = true;
+   return PPI_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+ppi_status ppi_batch_create(const ppi_gpu_config* c, int32_t n_pops, const ppi_batch_population* pops,
+                            ppi_batch** out) {
+   if (!c || !pops || !out || n_pops < 1 || c->max_size < 1 || c->max_size > 65535 || c->math < 0 ||
+       c->math > 2 || c->n_symbols < 0 || (c->n_symbols > 0 && !c->symbols))
+      return PPI_ERR_INVALID_ARGUMENT;
+   *out = nullptr;
+   long long total = 0;
+   for (int p = 0; p < n_pops; ++p) {
+      const ppi_batch_population& q = pops[p];
+      if (!q.rows || q.nlin < 1 || q.ncol < 1 || q.n < 1 || q.strategy < 0 || q.strategy > 2 ||
+          q.error_fn < 0 || q.error_fn > 3 || q.lanes > kMaxLanes ||
+          (q.error_fn == PPI_EF_COST && (!q.cost || q.cost_n < 1 || q.cost_n > 4096)))
+         return PPI_ERR_INVALID_ARGUMENT;
+      total += q.n;
+   }
+   if (total > (1 << 30)) return PPI_ERR_UNSUPPORTED;
+   ppi_batch* b = new ppi_batch();
+   auto bail = [&](ppi_status s) { bfree_all(b); delete b; return s; };
+   int ndev = 0;
+   if (cudaGetDeviceCount(&ndev) != cudaSuccess || c->device < 0 || c->device >= ndev) return bail(PPI_ERR_CUDA);
+   if (cudaSetDevice(c->device) != cudaSuccess) return bail(PPI_ERR_CUDA);
+   b->device = c->device;
+   cudaDeviceGetAttribute(&b->sm_count, cudaDevAttrMultiProcessorCount, c->device);
+   b->math = c->math;
+   b->max_size = c->max_size;
+   b->code_stride = 2 * c->max_size + 2;
+   b->n_pops = n_pops;
+   b->total = (int)total;
+   b->opset = opset_for(c->symbols, c->n_symbols);
+   if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
+       cudaEventCreate(&b->ev0) != cudaSuccess || cudaEventCreate(&b->ev1) != cudaSuccess)
+      return bail(PPI_ERR_CUDA);
+   // symbol table (as ppi_gpu_create)
+   int mn = 0, mx = -1;
+   for (int i = 0; i < c->n_symbols; ++i) {
+      if (c->symbols[i].op < 0 || c->symbols[i].op >= PPI_OP_COUNT) return bail(PPI_ERR_INVALID_ARGUMENT);
+      if (i == 0 || c->symbols[i].symbol < mn) mn = c->symbols[i].symbol;
+      if (i == 0 || c->symbols[i].symbol > mx) mx = c->symbols[i].symbol;
+   }
+   if (c->n_symbols > 0 && (long long)mx - mn + 1 > (1 << 22)) return bail(PPI_ERR_UNSUPPORTED);
+   std::vector<int2> lut(c->n_symbols > 0 ? (size_t)(mx - mn + 1) : 1, make_int2(PPI_OP_INVALID, 0x7fc00000));
+   for (int i = 0; i < c->n_symbols; ++i) {
+      int32_t bits;
+      std::memcpy(&bits, &c->symbols[i].value, 4);
+      lut[(size_t)(c->symbols[i].symbol - mn)] = make_int2(c->symbols[i].op, bits);
+   }
+   b->lut_min = mn;
+   b->lut_len = c->n_symbols > 0 ? mx - mn + 1 : 0;
+   if (balloc(&b->d_lut, lut.size()) != cudaSuccess ||
+       cudaMemcpy(b->d_lut, lut.data(), lut.size() * sizeof(int2), cudaMemcpyHostToDevice) != cudaSuccess)
+      return bail(PPI_ERR_OUT_OF_MEMORY);
+   // datasets (column-major, padded) and population descriptors
+   std::vector<int> pop_of((size_t)total);
+   int begin = 0;
+   for (int p = 0; p < n_pops; ++p) {
+      const ppi_batch_population& q = pops[p];
+      const int ld = (q.nlin + kColumnPad - 1) / kColumnPad * kColumnPad;
+      std::vector<float> cm((size_t)ld * q.ncol, 0.0f);
+      for (int i = 0; i < q.nlin; ++i)
+         for (int k = 0; k < q.ncol; ++k) cm[(size_t)k * ld + i] = q.rows[(size_t)i * q.ncol + k];
+      float* d = nullptr;
+      if (balloc(&d, cm.size()) != cudaSuccess) return bail(PPI_ERR_OUT_OF_MEMORY);
+      b->datasets.push_back(d);
+      if (cudaMemcpy(d, cm.data(), cm.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess) return bail(PPI_ERR_CUDA);
+      float* dc = nullptr;
+      if (q.error_fn == PPI_EF_COST) {
+         if (balloc(&dc, (size_t)q.cost_n * q.cost_n) != cudaSuccess) return bail(PPI_ERR_OUT_OF_MEMORY);
+         b->costs.push_back(dc);
+         if (cudaMemcpy(dc, q.cost, (size_t)q.cost_n * q.cost_n * 4, cudaMemcpyHostToDevice) != cudaSuccess)
+            return bail(PPI_ERR_CUDA);
+      }
+      b->max_ncol = std::max(b->max_ncol, q.ncol);
+      PopDesc pd{};
+      pd.data = d; pd.nlin = q.nlin; pd.ncol = q.ncol; pd.ld = ld;
+      pd.strategy = q.strategy; pd.lanes = resolve_lanes(q.strategy, q.lanes, q.nlin, b->sm_count);
+      pd.ef = q.error_fn; pd.reduce_max = q.reduce_max ? 1 : 0; pd.prot = q.protected_fns ? 1 : 0;
+      pd.cost = dc; pd.cost_n = q.error_fn == PPI_EF_COST ? q.cost_n : 0; pd.alpha = 0.0f;
+      pd.prog_begin = begin; pd.n = q.n;
+      if (pd.lanes < 1 || pd.lanes > kMaxLanes) return bail(PPI_ERR_UNSUPPORTED);
+      b->host_pops.push_back(pd);
+      for (int i = 0; i < q.n; ++i) pop_of[(size_t)begin + i] = p;
+      begin += q.n;
+   }
+   const size_t T = (size_t)b->total, ms = (size_t)c->max_size;
+   if (balloc(&b->d_pops, n_pops) != cudaSuccess || balloc(&b->d_pop_of, T) != cudaSuccess ||
+       balloc(&b->d_order, T) != cudaSuccess || balloc(&b->d_bucket_of, T) != cudaSuccess ||
+       balloc(&b->d_bucket, 2 * kBuckets) != cudaSuccess || balloc(&b->d_n_main, 1) != cudaSuccess ||
+       balloc(&b->d_pop_key, n_pops) != cudaSuccess ||
+       balloc(&b->d_pop_done, n_pops) != cudaSuccess || balloc(&b->d_best, n_pops) != cudaSuccess ||
+       balloc(&b->d_stats, 1) != cudaSuccess || balloc(&b->d_key, 1) != cudaSuccess ||
+       balloc(&b->d_status, 1) != cudaSuccess || balloc(&b->d_ph, T * ms) != cudaSuccess ||
+       balloc(&b->d_eph, T * ms) != cudaSuccess || balloc(&b->d_size, T) != cudaSuccess ||
+       balloc(&b->d_fit, T) != cudaSuccess || balloc(&b->d_code, T * b->code_stride) != cudaSuccess ||
+       balloc(&b->d_meta, T) != cudaSuccess || balloc(&b->d_work, T * 2 * ms) != cudaSuccess ||
+       cudaMallocHost(reinterpret_cast<void**>(&b->h_fit), T * 4) != cudaSuccess ||
+       cudaMallocHost(reinterpret_cast<void**>(&b->h_best), (size_t)n_pops * 4) != cudaSuccess ||
+       cudaMallocHost(reinterpret_cast<void**>(&b->h_status), 4) != cudaSuccess ||
+       cudaMallocHost(reinterpret_cast<void**>(&b->h_rows), kRowBins * sizeof(unsigned long long)) != cudaSuccess)
+      return bail(PPI_ERR_OUT_OF_MEMORY);
+   if (cudaMemcpy(b->d_pops, b->host_pops.data(), n_pops * sizeof(PopDesc), cudaMemcpyHostToDevice) != cudaSuccess ||
+       cudaMemcpy(b->d_pop_of, pop_of.data(), T * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess)
+      return bail(PPI_ERR_CUDA);
+   // default shape until tuned: 128 threads if it fits, else 64
+   if (batch_geometry(b, 128, 0, &b->geo) != PPI_OK && batch_geometry(b, 64, 0, &b->geo) != PPI_OK)
+      return bail(PPI_ERR_UNSUPPORTED);
+   *out = b;
+   return PPI_OK;
+}
+
+ppi_status ppi_batch_destroy(ppi_batch* b) {
+   if (!b) return PPI_ERR_INVALID_ARGUMENT;
+   cudaSetDevice(b->device);
+   if (b->stream) cudaStreamSynchronize(b->stream);
+   bfree_all(b);
+   delete b;
+   return PPI_OK;
+}
+
+const char* ppi_batch_last_error(const ppi_batch* b) { return b ? b->err.c_str() : "null handle"; }
+
+ppi_status ppi_batch_set_alpha(ppi_batch* b, const float* alpha) {
+   if (!b || !alpha) return PPI_ERR_INVALID_ARGUMENT;
+   PPI_BCUDA(b, cudaSetDevice(b->device));
+   for (int p = 0; p < b->n_pops; ++p) b->host_pops[p].alpha = alpha[p];
+   PPI_BCUDA(b, cudaMemcpy(b->d_pops, b->host_pops.data(), b->n_pops * sizeof(PopDesc), cudaMemcpyHostToDevice));
+   return PPI_OK;
+}
+
+ppi_status ppi_batch_evaluate_device(ppi_batch* b, const int32_t* d_ph, const float* d_eph,
+                                     const int32_t* d_size, float* d_fit, int32_t* d_best,
+                                     void* stream, int32_t flags) {
+   if (!b || !d_ph || !d_eph || !d_size || !d_fit || !d_best) return PPI_ERR_INVALID_ARGUMENT;
+   PPI_BCUDA(b, cudaSetDevice(b->device));
+   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+   if ((flags & PPI_BATCH_AUTOTUNE) && !b->tuned) {
+      ppi_status st = autotune(b, d_ph, d_eph, d_size, d_fit, d_best, s);
+      if (st != PPI_OK) return st;
+   }
+   const bool use_graph = (flags & PPI_BATCH_GRAPH) && s != nullptr;
+   if (!use_graph) {
+      PPI_BCUDA(b, cudaEventRecord(b->ev0, s));
+      ppi_status st = enqueue_step(b, d_ph, d_eph, d_size, d_fit, d_best, s, b->geo);
+      if (st != PPI_OK) return st;
+      PPI_BCUDA(b, cudaEventRecord(b->ev1, s));
+      return PPI_OK;
+   }
+   const void* key[6] = {d_ph, d_eph, d_size, d_fit, d_best,
+                         reinterpret_cast<void*>((size_t)b->geo.block << 16 | (size_t)b->geo.rows)};
+   if (!b->graph || std::memcmp(key, b->graph_key, sizeof key) != 0 || b->graph_stream != s) {
+      if (b->graph) {
+         cudaGraphExecDestroy(b->graph);
+         b->graph = nullptr;
+      }
+      cudaGraph_t g = nullptr;
+      PPI_BCUDA(b, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+      ppi_status st = enqueue_step(b, d_ph, d_eph, d_size, d_fit, d_best, s, b->geo);
+      cudaError_t ce = cudaStreamEndCapture(s, &g);
+      if (st != PPI_OK) {
+         if (g) cudaGraphDestroy(g);
+         return st;
+      }
+      PPI_BCUDA(b, ce);
+      ce = cudaGraphInstantiate(&b->graph, g, 0);
+      cudaGraphDestroy(g);
+      PPI_BCUDA(b, ce);
+      std::memcpy(b->graph_key, key, sizeof key);
+      b->graph_stream = s;
+   }
+   PPI_BCUDA(b, cudaEventRecord(b->ev0, s));
+   PPI_BCUDA(b, cudaGraphLaunch(b->graph, s));
+   PPI_BCUDA(b, cudaEventRecord(b->ev1, s));
+   return PPI_OK;
+}
+
+ppi_status ppi_batch_evaluate(ppi_batch* b, const int32_t* ph, const float* eph, const int32_t* size,
+                              float* fitness, int32_t* best_index, int32_t flags) {
+   if (!b || !ph || !eph || !size || !fitness) return PPI_ERR_INVALID_ARGUMENT;
+   PPI_BCUDA(b, cudaSetDevice(b->device));
+   const size_t T = (size_t)b->total, ms = (size_t)b->max_size;
+   PPI_BCUDA(b, cudaMemcpyAsync(b->d_ph, ph, T * ms * 4, cudaMemcpyHostToDevice, b->stream));
+   PPI_BCUDA(b, cudaMemcpyAsync(b->d_eph, eph, T * ms * 4, cudaMemcpyHostToDevice, b->stream));
+   PPI_BCUDA(b, cudaMemcpyAsync(b->d_size, size, T * 4, cudaMemcpyHostToDevice, b->stream));
+   ppi_status st = ppi_batch_evaluate_device(b, b->d_ph, b->d_eph, b->d_size, b->d_fit, b->d_best,
+                                             b->stream, flags);
+   if (st != PPI_OK) return st;
+   PPI_BCUDA(b, cudaMemcpyAsync(b->h_fit, b->d_fit, T * 4, cudaMemcpyDeviceToHost, b->stream));
+   PPI_BCUDA(b, cudaMemcpyAsync(b->h_best, b->d_best, (size_t)b->n_pops * 4, cudaMemcpyDeviceToHost, b->stream));
+   PPI_BCUDA(b, cudaMemcpyAsync(b->h_status, b->d_status, 4, cudaMemcpyDeviceToHost, b->stream));
+   PPI_BCUDA(b, cudaStreamSynchronize(b->stream));
+   std::memcpy(fitness, b->h_fit, T * 4);
+   if (best_index) std::memcpy(best_index, b->h_best, (size_t)b->n_pops * 4);
+   cudaEventElapsedTime(&b->last_ms, b->ev0, b->ev1);
+   if (*b->h_status & kStatusUnsupportedProgram)
+      return bfail(b, PPI_ERR_UNSUPPORTED, "a malformed program needs a deeper stack than supported");
+   return PPI_OK;
+}
+
+ppi_status ppi_batch_last_kernel_ms(ppi_batch* b, float* ms) {
+   if (!b || !ms) return PPI_ERR_INVALID_ARGUMENT;
+   PPI_BCUDA(b, cudaEventSynchronize(b->ev1));
+   PPI_BCUDA(b, cudaEventElapsedTime(ms, b->ev0, b->ev1));
+   return PPI_OK;
+}
+
+ppi_status ppi_batch_shape(const ppi_batch* b, int32_t* block, int32_t* grid, float* tune_ms) {
+   if (!b || !block || !grid) return PPI_ERR_INVALID_ARGUMENT;
+   *block = b->geo.block;
+   *grid = b->geo.grid;
+   if (tune_ms) {
+      tune_ms[0] = b->tune_ms[0];
+      tune_ms[1] = b->tune_ms[1];
+   }
+   return PPI_OK;
+}
+
+}  // extern "C"

@@ -14,16 +14,22 @@ cudaError_t launch_evaluate_native(int opset, const EvalArgs& a, int block, int 
 cudaError_t launch_predict_fast(int opset, const PredictArgs& a, int block, int grid, size_t smem, cudaStream_t s);
 cudaError_t launch_predict_parity(int opset, const PredictArgs& a, int block, int grid, size_t smem, cudaStream_t s);
 cudaError_t launch_predict_native(int opset, const PredictArgs& a, int block, int grid, size_t smem, cudaStream_t s);
+cudaError_t launch_evaluate_batch_fast(int opset, const BatchArgs& a, int block, int grid, size_t smem, cudaStream_t s);
+cudaError_t launch_evaluate_batch_parity(int opset, const BatchArgs& a, int block, int grid, size_t smem, cudaStream_t s);
+cudaError_t launch_evaluate_batch_native(int opset, const BatchArgs& a, int block, int grid, size_t smem, cudaStream_t s);
 cudaError_t evaluate_occupancy_fast(int opset, int block, size_t smem, int* per_sm);
 cudaError_t evaluate_occupancy_parity(int opset, int block, size_t smem, int* per_sm);
 cudaError_t evaluate_occupancy_native(int opset, int block, size_t smem, int* per_sm);
+cudaError_t evaluate_batch_occupancy_fast(int opset, int block, size_t smem, int* per_sm);
+cudaError_t evaluate_batch_occupancy_parity(int opset, int block, size_t smem, int* per_sm);
+cudaError_t evaluate_batch_occupancy_native(int opset, int block, size_t smem, int* per_sm);
 
-size_t evaluate_smem_bytes(int code_stride, int ncol, int block, int R, int lanes, bool aligned) {
+size_t evaluate_smem_bytes(int code_stride, int rows, int block, int R, int lanes, bool aligned) {
    const size_t T = (size_t)block * R;
    const size_t code = ((size_t)(code_stride + 1) * sizeof(uint2) + 15) & ~(size_t)15;
-   const size_t rows = (size_t)(ncol + kSlots) * T * 4;
-   if (aligned) return code + std::max(rows, (size_t)lanes * 4);
-   return code + rows + T * 4 + (size_t)lanes * 8;
+   const size_t tile = (size_t)std::max(rows, 1) * T * 4;
+   if (aligned) return code + tile;   // lane values reuse the tile
+   return code + tile + (size_t)lanes * 4 + (((size_t)lanes + 15) & ~(size_t)15);
 }
 
 cudaError_t launch_evaluate(int math, int opset, const EvalArgs& a, int block, int grid, size_t smem,
@@ -44,11 +50,28 @@ cudaError_t launch_predict(int math, int opset, const PredictArgs& a, int block,
    }
 }
 
+cudaError_t launch_evaluate_batch(int math, int opset, const BatchArgs& a, int block, int grid,
+                                  size_t smem, cudaStream_t s) {
+   switch (math) {
+   case kMathParity: return launch_evaluate_batch_parity(opset, a, block, grid, smem, s);
+   case kMathNative: return launch_evaluate_batch_native(opset, a, block, grid, smem, s);
+   default: return launch_evaluate_batch_fast(opset, a, block, grid, smem, s);
+   }
+}
+
 cudaError_t evaluate_occupancy(int math, int opset, int block, size_t smem, int* per_sm) {
    switch (math) {
    case kMathParity: return evaluate_occupancy_parity(opset, block, smem, per_sm);
    case kMathNative: return evaluate_occupancy_native(opset, block, smem, per_sm);
    default: return evaluate_occupancy_fast(opset, block, smem, per_sm);
+   }
+}
+
+cudaError_t evaluate_batch_occupancy(int math, int opset, int block, size_t smem, int* per_sm) {
+   switch (math) {
+   case kMathParity: return evaluate_batch_occupancy_parity(opset, block, smem, per_sm);
+   case kMathNative: return evaluate_batch_occupancy_native(opset, block, smem, per_sm);
+   default: return evaluate_batch_occupancy_fast(opset, block, smem, per_sm);
    }
 }
 
@@ -78,12 +101,13 @@ int resolve_lanes(int strategy, int lanes, int nlin, int sm_count) {
 }
 
 const char* plan_geometry(int strategy, int lanes, int math, int opset, int nlin, int ncol,
-                          int code_stride, int n_max, int sm_count, Geometry* g) {
+                          int code_stride, int n_max, int sm_count, Geometry* g, int rows_hint) {
    const int L = lanes;
    if (L < 1 || L > kMaxLanes) return "lane count out of range";
    // records per thread: kR (8 measured faster than 16 on GB300: more
    // resident warps hide the dispatch latency)
    const int R = kR;
+   constexpr size_t kSmemCap = 200 * 1024;
    int P;
    if (strategy == PPI_STRATEGY_PDP && L % (32 * R) == 0 && L / R <= 128) {
       P = L / R;   // lane == tile position: register accumulation
@@ -93,24 +117,67 @@ const char* plan_geometry(int strategy, int lanes, int math, int opset, int nlin
    }
    if (strategy == PPI_STRATEGY_DP && L > P * R)
       return "DP lanes above 1024 records per group are not supported";
-   bool aligned = strategy == PPI_STRATEGY_PDP && L == P * R;
-   size_t smem = evaluate_smem_bytes(code_stride, ncol, P, R, L, aligned);
-   while (smem > 200 * 1024 && P > 32 && !(strategy == PPI_STRATEGY_DP && L > (P / 2) * R)) {
+   const int rows_max = max_program_rows(ncol);
+   // wide budget: every program row count up to rows_max if it fits in
+   // kSmemCap, else as many rows as fit (programs needing more take the
+   // generic form); a narrower block when not even one column fits
+   auto aligned_for = [&](int p) { return strategy == PPI_STRATEGY_PDP && L == p * R; };
+   auto rows_fit = [&](int p) {
+      const size_t fixed = evaluate_smem_bytes(code_stride, 0, p, R, L, aligned_for(p)) -
+                           (size_t)p * R * 4;
+      if (fixed >= kSmemCap) return 0;
+      return (int)std::min<size_t>((kSmemCap - fixed) / ((size_t)p * R * 4), 4096);
+   };
+   while (P > 32 && rows_fit(P) < std::min(rows_max, kSlots + 2) &&
+          !(strategy == PPI_STRATEGY_DP && L > (P / 2) * R))
       P /= 2;
-      aligned = strategy == PPI_STRATEGY_PDP && L == P * R;
-      smem = evaluate_smem_bytes(code_stride, ncol, P, R, L, aligned);
-   }
-   if (smem > 200 * 1024) return "dataset has too many columns for one shared-memory tile";
-   int per_sm = 0;
-   if (evaluate_occupancy(math, opset, P, smem, &per_sm) != cudaSuccess || per_sm < 1)
-      return "evaluator does not fit on an SM";
+   const bool aligned = aligned_for(P);
+   const int rows_wide = std::min(rows_max, rows_fit(P));
+   if (rows_wide < 1) return "lane buffers do not fit in shared memory";
+   auto occupancy = [&](int rows) {
+      int per_sm = 0;
+      const size_t smem = evaluate_smem_bytes(code_stride, rows, P, R, L, aligned);
+      if (evaluate_occupancy(math, opset, P, smem, &per_sm) != cudaSuccess) return 0;
+      return per_sm;
+   };
+   // main budget: the most rows at the occupancy of a one-row tile, or the
+   // hint when it asks for more
+   const int top = occupancy(1);
+   if (top < 1) return "evaluator does not fit on an SM";
+   int rows = 1;
+   while (rows < rows_wide && occupancy(rows + 1) >= top) ++rows;
+   if (rows_hint > rows) rows = std::min(rows_hint, rows_wide);
    g->lanes = L;
    g->block = P;
    g->R = R;
    g->opset = opset;
-   g->smem = smem;
-   g->grid = std::max(1, std::min(n_max, per_sm * sm_count));
+   g->aligned = aligned;
+   g->rows = rows;
+   g->smem = evaluate_smem_bytes(code_stride, rows, P, R, L, aligned);
+   g->per_sm[0] = occupancy(rows);
+   if (g->per_sm[0] < 1) return "evaluator does not fit on an SM";
+   g->grid = std::max(1, std::min(n_max, g->per_sm[0] * sm_count));
+   g->wide = rows < rows_wide;
+   g->rows_wide = rows_wide;
+   g->smem_wide = evaluate_smem_bytes(code_stride, rows_wide, P, R, L, aligned);
+   g->per_sm[1] = occupancy(rows_wide);
+   if (g->per_sm[1] < 1) return "evaluator does not fit on an SM";
+   g->grid_wide = std::max(1, std::min(n_max, g->per_sm[1] * sm_count));
    return nullptr;
+}
+
+int rows_for_histogram(const unsigned long long* rows_work, int rows_cap, double spill) {
+   double total = 0.0;
+   for (int r = 0; r < kRowBins; ++r) total += (double)rows_work[r];
+   if (total <= 0.0) return 1;
+   double above = total;
+   int r = 0;
+   while (r < kRowBins - 1) {
+      above -= (double)rows_work[r];
+      if (above <= spill * total) break;
+      ++r;
+   }
+   return std::max(1, std::min(r, rows_cap));
 }
 
 }  // namespace ppi

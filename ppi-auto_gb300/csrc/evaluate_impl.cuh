@@ -4,8 +4,10 @@
 //   * one CTA of P threads evaluates one program at a time, pulling program
 //     indices from a device work queue (persistent grid, one wave of CTAs);
 //   * the dataset is column-major in HBM; each CTA stages a tile of
-//     T = P * R records (all columns) into shared memory with 16-byte
-//     vector loads, so attribute reads are conflict-free LDS.128;
+//     T = P * R records into shared memory with 16-byte vector loads: only
+//     the columns the program reads (listed by the translator) and the
+//     target, so shared memory per CTA follows the program, not the dataset
+//     width, and attribute reads are conflict-free LDS.128;
 //   * the program's bytecode sits in shared memory and every warp walks it in
 //     lock step: instruction dispatch is warp-uniform (no divergence) and each
 //     instruction is applied to the R records a thread holds in its
@@ -18,7 +20,10 @@
 //       DP: per-group trees in shared memory, groups added in order;
 //     then the reference's local tree (accelerator.cl:157-167, 252-262);
 //   * fitness, alpha*size and the arg-min (64-bit packed atomicMin) are fused
-//     into the same kernel; the last CTA to finish writes the best index.
+//     into the same kernel; the last CTA to finish writes the best index;
+//   * two passes with different shared-memory budgets: the main pass runs
+//     every program whose tile fits its row budget (sized for occupancy),
+//     the wide pass the few that need more rows.
 #pragma once
 
 #include "ppi_internal.cuh"
@@ -125,9 +130,12 @@ __device__ __forceinline__ float generic_op(int op, float a, float b, int prot) 
 
 // Right-to-left stack evaluation with the reference's stack semantics
 // (accelerator.cl:28-53); missing operands of a malformed program read as NaN.
+// Attribute reads go straight to the dataset in global memory (positions at
+// or past ld read 0, as the staged tile does).
 template <int MATH, int R>
-__device__ __noinline__ void run_generic(const uint2* __restrict__ code, const float* __restrict__ tile,
-                                         int T, int P, int tid, float* __restrict__ out, int prot) {
+__device__ __noinline__ void run_generic(const uint2* __restrict__ code, const float* __restrict__ data,
+                                         int ld, int base, int P, int tid, float* __restrict__ out,
+                                         int prot) {
    float stk[kGenericStack];
    const float qnan = __uint_as_float(0x7fc00000u);
 #pragma unroll 1
@@ -148,7 +156,7 @@ __device__ __noinline__ void run_generic(const uint2* __restrict__ code, const f
          }
          if (ar == 0) {
             float v;
-            if (op == PPI_OP_ATTRIBUTE) v = tile[(size_t)ins.y * T + rec];
+            if (op == PPI_OP_ATTRIBUTE) v = (base + rec < ld) ? __ldg(data + (size_t)ins.y * ld + base + rec) : 0.0f;
             else v = __uint_as_float(ins.y);   // CONST / LITERAL value, INVALID = NaN
             stk[++top] = v;
          } else if (ar == 3) {
@@ -165,18 +173,24 @@ __device__ __noinline__ void run_generic(const uint2* __restrict__ code, const f
    }
 }
 
-__device__ __forceinline__ void stage_tile(const EvalArgs& a, float* s_tile, int base, int T,
-                                           int tid, int P) {
+// Stage the records [base, base + T) of the program's columns (tile rows
+// s .. s+k-1, from the code header) and of the target column (row s+k).
+__device__ __forceinline__ void stage_tile(const float* data, int ncol, int ld, const uint2* s_code,
+                                           float* s_tile, int base, int T, int tid, int P) {
    const bool vec = (base & 3) == 0;
-   for (int cidx = 0; cidx < a.ncol; ++cidx) {
-      const float* src = a.data + (size_t)cidx * a.ld + base;
-      float* dst = s_tile + (size_t)cidx * T;
+   const uint2 hdr = s_code[0];
+   const int k = (int)hdr.x, s = (int)hdr.y;
+   for (int j = 0; j <= k; ++j) {
+      const uint2 pair = s_code[1 + (j >> 1)];
+      const int cidx = (j == k) ? ncol - 1 : (int)((j & 1) ? pair.y : pair.x);
+      const float* src = data + (size_t)cidx * ld + base;
+      float* dst = s_tile + (size_t)(s + j) * T;
       for (int t = tid * 4; t < T; t += P * 4) {
-         if (vec && base + t + 3 < a.ld) {
+         if (vec && base + t + 3 < ld) {
             *reinterpret_cast<float4*>(dst + t) = __ldg(reinterpret_cast<const float4*>(src + t));
          } else {
 #pragma unroll
-            for (int j = 0; j < 4; ++j) dst[t + j] = (base + t + j < a.ld) ? __ldg(src + t + j) : 0.0f;
+            for (int j = 0; j < 4; ++j) dst[t + j] = (base + t + j < ld) ? __ldg(src + t + j) : 0.0f;
          }
       }
    }
@@ -207,160 +221,252 @@ __device__ __forceinline__ void local_tree(float* pe, int L, int reduce_max, int
    }
 }
 
+// Everything the evaluation of one program needs (one population's dataset
+// and error settings, the program's translation).
+struct Job {
+   const float* data;
+   int nlin, ncol, ld;
+   int strategy, lanes, ef, reduce_max, prot, cost_n;
+   const float* cost;
+   float alpha;
+   int2 meta;                  // {kind | rows << 8, code length}
+   int size;
+   const uint2* code;          // in global memory
+   int rows_cap;               // tile rows of this pass (lane accumulators follow them)
+};
+
+// Fitness of one program (valid in thread 0), in exactly the reference
+// strategy's accumulation order.  All threads of the CTA call it; it starts
+// and ends with the CTA synchronised.  s_code/s_tile: shared memory; the rows
+// region holds job.rows_cap rows of T = P*R floats (slots, staged columns,
+// target; row 0 is reused for the tile's errors once the program has run),
+// then, unless the lane == tile-position path applies, lanes floats of lane
+// accumulators and lanes bytes of lane-finished flags.
+template <int MATH, int R, int OPSET>
+__device__ float evaluate_program(const Job& j, uint2* s_code, float* s_tile, int* status, int tid,
+                                  int P) {
+   const int T = P * R;
+   const int L = j.lanes;
+   const bool aligned = j.strategy == PPI_STRATEGY_PDP && L == T;
+   const bool dp = j.strategy == PPI_STRATEGY_DP;
+   const int kind = meta_kind(j.meta);
+   float* s_err = s_tile;
+   // the aligned path needs no error/lane buffers: its final lane values
+   // reuse the start of the rows region once the last tile is done
+   float* s_acc = aligned ? s_tile : s_tile + (size_t)j.rows_cap * T;
+   unsigned char* s_done = reinterpret_cast<unsigned char*>(s_acc + L);
+   const int Teff = dp ? L * (T / L) : T;
+   const float fnlin = (float)j.nlin;
+   float fit = FLT_MAX;
+   if (kind == kKindInvalid || kind == kKindUnsupported) {
+      // size 0 (sizes outside [1, max_size] are treated as 0)
+      if (tid == 0) {
+         if (kind == kKindUnsupported) atomicOr(status, kStatusUnsupportedProgram);
+         if (kind == kKindInvalid && dp) {
+            // every group reports MAXFLOAT (accelerator.cl:108-112); host rule
+            float sum = 0.0f;
+            const int G = (j.nlin + L - 1) / L;
+            for (int g = 0; g < G; ++g) sum = reduce1(j.reduce_max, sum, FLT_MAX, fnlin);
+            fit = nonfinite(sum) ? FLT_MAX : sum / fnlin;
+         }
+      }
+      __syncthreads();
+      return fit;
+   }
+   for (int i = tid; i < j.meta.y; i += P) s_code[i] = j.code[i];
+   if (!aligned)
+      for (int l = tid; l < L; l += P) { s_acc[l] = 0.0f; s_done[l] = 0; }
+   const uint2* prog = s_code + code_header((int)j.code[0].x);
+   const int trow = (int)(j.code[0].x + j.code[0].y);
+   float lacc[R];
+#pragma unroll
+   for (int r = 0; r < R; ++r) lacc[r] = 0.0f;
+   uint32_t ldone = 0u;
+   float dsum = 0.0f;
+   bool ddone = false;
+   for (int base = 0; base < j.nlin; base += Teff) {
+      __syncthreads();
+      stage_tile(j.data, j.ncol, j.ld, s_code, s_tile, base, T, tid, P);
+      __syncthreads();
+      float v[R];
+      if (kind != kKindGeneric) {
+         run_fast<MATH, R, OPSET>(prog, s_tile + tid * 4, T, P, v, j.prot);
+      } else {
+         float tmp[R];
+         run_generic<MATH, R>(prog, j.data, j.ld, base, P, tid, tmp, j.prot);
+#pragma unroll
+         for (int r = 0; r < R; ++r) v[r] = tmp[r];
+      }
+      float ycol[R];
+      load_row(s_tile + (size_t)trow * T + tid * 4, P, ycol);
+      float e[R];
+#pragma unroll
+      for (int r = 0; r < R; ++r) e[r] = apply_error(j.ef, v[r], ycol[r], j.cost, j.cost_n);
+      if (aligned) {
+#pragma unroll
+         for (int r = 0; r < R; ++r) {
+            const int n = base + tile_pos(tid, r, P);
+            if (n < j.nlin && !((ldone >> r) & 1u)) {
+               if (nonfinite(e[r])) { lacc[r] = FLT_MAX; ldone |= 1u << r; }
+               else lacc[r] = reduce1(j.reduce_max, lacc[r], e[r], fnlin);
+            }
+         }
+      } else {
+         __syncthreads();   // every thread is done with the rows: row 0 takes the errors
+#pragma unroll
+         for (int r = 0; r < R; ++r) {
+            const int t = tile_pos(tid, r, P);
+            s_err[t] = (dp && base + t >= j.nlin) ? 0.0f : e[r];
+         }
+         __syncthreads();
+         if (dp) {
+            const int G = Teff / L;
+            int p2 = 1;
+            while (p2 < L) p2 <<= 1;
+            for (int s = p2 >> 1; s > 0; s >>= 1) {
+               for (int idx = tid; idx < G * s; idx += P) {
+                  const int gi = idx / s, l = idx - gi * s;
+                  if (l + s < L) {
+                     float* pe = s_err + gi * L;
+                     pe[l] = j.reduce_max ? ((pe[l + s] > pe[l]) ? pe[l + s] : pe[l]) : pe[l] + pe[l + s];
+                  }
+               }
+               __syncthreads();
+            }
+            if (tid == 0) {
+               for (int gi = 0; gi < G && !ddone; ++gi) {
+                  if (base + gi * L >= j.nlin) break;
+                  const float part = s_err[gi * L];
+                  if (nonfinite(part)) { dsum = FLT_MAX; ddone = true; }
+                  else dsum = reduce1(j.reduce_max, dsum, part, fnlin);
+               }
+            }
+         } else {
+            const int end = min(base + T, j.nlin);
+            const int off = base % L;
+            for (int l = tid; l < L; l += P) {
+               if (s_done[l]) continue;
+               float acc = s_acc[l];
+               int done = 0;
+               for (int n = base + (l - off + L) % L; n < end; n += L) {
+                  const float ev = s_err[n - base];
+                  if (nonfinite(ev)) { acc = FLT_MAX; done = 1; break; }
+                  acc = reduce1(j.reduce_max, acc, ev, fnlin);
+               }
+               s_acc[l] = acc;
+               if (done) s_done[l] = 1;
+            }
+         }
+      }
+   }
+   __syncthreads();
+   if (dp) {
+      if (tid == 0) fit = nonfinite(dsum) ? FLT_MAX : dsum / fnlin + j.alpha * (float)j.size;
+   } else {
+      if (aligned) {
+         __syncthreads();   // every thread is done with the rows region
+#pragma unroll
+         for (int r = 0; r < R; ++r) s_acc[tile_pos(tid, r, P)] = lacc[r];
+         __syncthreads();
+      }
+      local_tree(s_acc, L, j.reduce_max, tid, P);
+      if (tid == 0) {
+         const float pe = s_acc[0];
+         const float vv = nonfinite(pe) ? FLT_MAX : pe / fnlin;
+         fit = vv + j.alpha * (float)j.size;
+      }
+   }
+   __syncthreads();
+   return fit;
+}
+
+// One population: a persistent grid pulls program indices from a device
+// counter; the last CTA to finish turns the packed arg-min into the index.
 template <int MATH, int R, int OPSET>
 __global__ void __launch_bounds__(128, 4) eval_kernel(const EvalArgs a) {
    extern __shared__ __align__(16) unsigned char smem_raw[];
    __shared__ int s_prog;
-   const int P = blockDim.x, tid = threadIdx.x, T = P * R;
-   const int L = a.lanes;
+   const int P = blockDim.x, tid = threadIdx.x;
    uint2* s_code = reinterpret_cast<uint2*>(smem_raw);
    float* s_tile = reinterpret_cast<float*>(smem_raw + code_bytes(a.code_stride));
-   const bool aligned = a.strategy == PPI_STRATEGY_PDP && L == T;
-   float* s_err = s_tile + (size_t)(a.ncol + kSlots) * T;
-   // the aligned path needs no error/lane buffers: its final lane values
-   // reuse the start of the rows region once the last tile is done
-   float* s_acc = aligned ? s_tile : s_err + T;
-   int* s_done = reinterpret_cast<int*>(s_acc + L);
-   const bool dp = a.strategy == PPI_STRATEGY_DP;
-   const int Teff = dp ? L * (T / L) : T;
-   const float fnlin = (float)a.nlin;
-
+   Job j;
+   j.data = a.data; j.nlin = a.nlin; j.ncol = a.ncol; j.ld = a.ld;
+   j.strategy = a.strategy; j.lanes = a.lanes; j.ef = a.ef; j.reduce_max = a.reduce_max;
+   j.prot = a.prot; j.cost = a.cost; j.cost_n = a.cost_n; j.alpha = a.alpha;
+   j.rows_cap = a.rows;
+   unsigned* queue = a.wide_pass ? &a.stats->wide_queue : &a.stats->queue;
+   const int limit = a.wide_pass ? (int)a.stats->wide : a.n;
    for (;;) {
-      if (tid == 0) s_prog = (int)atomicAdd(&a.counters[0], 1u);
+      if (tid == 0) s_prog = (int)atomicAdd(queue, 1u);
       __syncthreads();
-      const int prog = s_prog;
-      if (prog >= a.n) break;
-      const int2 m = a.meta[prog];
-      const int size = a.size[prog];
-      float fit = FLT_MAX;
-      if (m.x == kKindInvalid || m.x == kKindUnsupported) {
-         // size 0 (sizes outside [1, max_size] are treated as 0)
-         if (tid == 0) {
-            if (m.x == kKindUnsupported) atomicOr(a.status, kStatusUnsupportedProgram);
-            if (m.x == kKindInvalid && dp) {
-               // every group reports MAXFLOAT (accelerator.cl:108-112); host rule
-               float sum = 0.0f;
-               const int G = (a.nlin + L - 1) / L;
-               for (int g = 0; g < G; ++g) sum = reduce1(a.reduce_max, sum, FLT_MAX, fnlin);
-               fit = nonfinite(sum) ? FLT_MAX : sum / fnlin;
-            }
-         }
-      } else {
-         const uint2* g = a.code + (size_t)prog * a.code_stride;
-         for (int i = tid; i < m.y; i += P) s_code[i] = g[i];
-         if (!aligned)
-            for (int l = tid; l < L; l += P) { s_acc[l] = 0.0f; s_done[l] = 0; }
-         float lacc[R];
-#pragma unroll
-         for (int r = 0; r < R; ++r) lacc[r] = 0.0f;
-         uint32_t ldone = 0u;
-         float dsum = 0.0f;
-         bool ddone = false;
-         for (int base = 0; base < a.nlin; base += Teff) {
-            __syncthreads();
-            stage_tile(a, s_tile, base, T, tid, P);
-            __syncthreads();
-            float v[R];
-            if (m.x == kKindFast) {
-               run_fast<MATH, R, OPSET>(s_code, s_tile + tid * 4, T, P, v, a.prot);
-            } else {
-               float tmp[R];
-               run_generic<MATH, R>(s_code, s_tile, T, P, tid, tmp, a.prot);
-#pragma unroll
-               for (int r = 0; r < R; ++r) v[r] = tmp[r];
-            }
-            float ycol[R];
-            load_row(s_tile + (size_t)(a.ncol - 1) * T + tid * 4, P, ycol);
-            float e[R];
-#pragma unroll
-            for (int r = 0; r < R; ++r) e[r] = apply_error(a.ef, v[r], ycol[r], a.cost, a.cost_n);
-            if (aligned) {
-#pragma unroll
-               for (int r = 0; r < R; ++r) {
-                  const int n = base + tile_pos(tid, r, P);
-                  if (n < a.nlin && !((ldone >> r) & 1u)) {
-                     if (nonfinite(e[r])) { lacc[r] = FLT_MAX; ldone |= 1u << r; }
-                     else lacc[r] = reduce1(a.reduce_max, lacc[r], e[r], fnlin);
-                  }
-               }
-            } else {
-#pragma unroll
-               for (int r = 0; r < R; ++r) {
-                  const int t = tile_pos(tid, r, P);
-                  s_err[t] = (dp && base + t >= a.nlin) ? 0.0f : e[r];
-               }
-               __syncthreads();
-               if (dp) {
-                  const int G = Teff / L;
-                  int p2 = 1;
-                  while (p2 < L) p2 <<= 1;
-                  for (int s = p2 >> 1; s > 0; s >>= 1) {
-                     for (int idx = tid; idx < G * s; idx += P) {
-                        const int gi = idx / s, l = idx - gi * s;
-                        if (l + s < L) {
-                           float* pe = s_err + gi * L;
-                           pe[l] = a.reduce_max ? ((pe[l + s] > pe[l]) ? pe[l + s] : pe[l]) : pe[l] + pe[l + s];
-                        }
-                     }
-                     __syncthreads();
-                  }
-                  if (tid == 0) {
-                     for (int gi = 0; gi < G && !ddone; ++gi) {
-                        if (base + gi * L >= a.nlin) break;
-                        const float part = s_err[gi * L];
-                        if (nonfinite(part)) { dsum = FLT_MAX; ddone = true; }
-                        else dsum = reduce1(a.reduce_max, dsum, part, fnlin);
-                     }
-                  }
-               } else {
-                  const int end = min(base + T, a.nlin);
-                  const int off = base % L;
-                  for (int l = tid; l < L; l += P) {
-                     if (s_done[l]) continue;
-                     float acc = s_acc[l];
-                     int done = 0;
-                     for (int n = base + (l - off + L) % L; n < end; n += L) {
-                        const float ev = s_err[n - base];
-                        if (nonfinite(ev)) { acc = FLT_MAX; done = 1; break; }
-                        acc = reduce1(a.reduce_max, acc, ev, fnlin);
-                     }
-                     s_acc[l] = acc;
-                     if (done) s_done[l] = 1;
-                  }
-               }
-            }
-         }
-         __syncthreads();
-         if (dp) {
-            if (tid == 0) fit = nonfinite(dsum) ? FLT_MAX : dsum / fnlin + a.alpha * (float)size;
-         } else {
-            if (aligned) {
-               __syncthreads();   // every thread is done with the rows region
-#pragma unroll
-               for (int r = 0; r < R; ++r) s_acc[tile_pos(tid, r, P)] = lacc[r];
-               __syncthreads();
-            }
-            local_tree(s_acc, L, a.reduce_max, tid, P);
-            if (tid == 0) {
-               const float pe = s_acc[0];
-               const float vv = nonfinite(pe) ? FLT_MAX : pe / fnlin;
-               fit = vv + a.alpha * (float)size;
-            }
-         }
+      const int item = s_prog;
+      if (item >= limit) break;
+      const int prog = a.wide_pass ? a.wide_list[item] : item;
+      j.meta = a.meta[prog];
+      if (!a.wide_pass && meta_kind(j.meta) == kKindWide) {
+         __syncthreads();   // s_prog is read by every thread before it is rewritten
+         continue;
       }
+      j.size = a.size[prog];
+      j.code = a.code + (size_t)prog * a.code_stride;
+      const float fit = evaluate_program<MATH, R, OPSET>(j, s_code, s_tile, a.status, tid, P);
       if (tid == 0) {
          a.fitness[prog] = fit;
          atomicMin(a.best_key, fitness_key(fit, prog));
       }
-      __syncthreads();
    }
-   if (tid == 0) {
+   if (a.final_pass && tid == 0) {
       __threadfence();
-      const unsigned done = atomicAdd(&a.counters[1], 1u);
+      const unsigned done = atomicAdd(&a.stats->finished, 1u);
       if (done == gridDim.x - 1) {
          __threadfence();
          const unsigned long long k = *reinterpret_cast<volatile unsigned long long*>(a.best_key);
          a.best_index[0] = (int32_t)(0xFFFFFFFFu - (uint32_t)(k & 0xFFFFFFFFull));
+      }
+   }
+}
+
+// Many populations in one persistent launch: work items are program indices
+// in cost order (size x records, largest first); each population keeps its
+// own arg-min key and completion counter, and the CTA that finishes a
+// population's last program writes that population's best index.
+template <int MATH, int R, int OPSET>
+__global__ void __launch_bounds__(128, 4) eval_batch_kernel(const BatchArgs a) {
+   extern __shared__ __align__(16) unsigned char smem_raw[];
+   __shared__ int s_item;
+   const int P = blockDim.x, tid = threadIdx.x;
+   uint2* s_code = reinterpret_cast<uint2*>(smem_raw);
+   float* s_tile = reinterpret_cast<float*>(smem_raw + code_bytes(a.code_stride));
+   const int lo = a.wide_pass ? (int)*a.n_main : 0;
+   const int hi = a.wide_pass ? a.total : (int)*a.n_main;
+   unsigned* queue = a.wide_pass ? &a.stats->wide_queue : &a.stats->queue;
+   for (;;) {
+      if (tid == 0) s_item = lo + (int)atomicAdd(queue, 1u);
+      __syncthreads();
+      const int item = s_item;
+      if (item >= hi) break;
+      const int g = a.order[item];
+      const int p = a.pop_of[g];
+      const PopDesc& pd = a.pops[p];
+      Job j;
+      j.data = pd.data; j.nlin = pd.nlin; j.ncol = pd.ncol; j.ld = pd.ld;
+      j.strategy = pd.strategy; j.lanes = pd.lanes; j.ef = pd.ef; j.reduce_max = pd.reduce_max;
+      j.prot = pd.prot; j.cost = pd.cost; j.cost_n = pd.cost_n; j.alpha = pd.alpha;
+      j.meta = a.meta[g];
+      j.size = a.size[g];
+      j.code = a.code + (size_t)g * a.code_stride;
+      j.rows_cap = a.rows;
+      const float fit = evaluate_program<MATH, R, OPSET>(j, s_code, s_tile, a.status, tid, P);
+      if (tid == 0) {
+         const int local = g - pd.prog_begin;
+         a.fitness[g] = fit;
+         atomicMin(&a.pop_key[p], fitness_key(fit, local));
+         __threadfence();
+         if (atomicAdd(&a.pop_done[p], 1u) == (unsigned)pd.n - 1) {
+            __threadfence();
+            const unsigned long long k = *reinterpret_cast<volatile unsigned long long*>(&a.pop_key[p]);
+            a.best_index[p] = (int32_t)(0xFFFFFFFFu - (uint32_t)(k & 0xFFFFFFFFull));
+         }
       }
    }
 }
@@ -374,21 +480,20 @@ __global__ void __launch_bounds__(128, 4) predict_kernel(const PredictArgs a) {
    uint2* s_code = reinterpret_cast<uint2*>(smem_raw);
    float* s_tile = reinterpret_cast<float*>(smem_raw + code_bytes(m.y));
    for (int i = tid; i < m.y; i += P) s_code[i] = a.code[i];
-   EvalArgs ea{};
-   ea.data = a.data;
-   ea.nlin = a.nlin;
-   ea.ncol = a.ncol;
-   ea.ld = a.ld;
+   const int kind = meta_kind(m);
+   const bool runs = kind == kKindFast || kind == kKindWide || kind == kKindGeneric;
+   const uint2* prog = s_code + (runs ? code_header((int)a.code[0].x) : 0);
    for (int base = blockIdx.x * T; base < a.nlin; base += gridDim.x * T) {
       __syncthreads();
-      stage_tile(ea, s_tile, base, T, tid, P);
+      if (runs)
+         stage_tile(a.data, a.ncol, a.ld, s_code, s_tile, base, T, tid, P);
       __syncthreads();
       float v[R];
-      if (m.x == kKindFast) {
-         run_fast<MATH, R, OPSET>(s_code, s_tile + tid * 4, T, P, v, a.prot);
-      } else if (m.x == kKindGeneric) {
+      if (kind == kKindFast || kind == kKindWide) {
+         run_fast<MATH, R, OPSET>(prog, s_tile + tid * 4, T, P, v, a.prot);
+      } else if (kind == kKindGeneric) {
          float tmp[R];
-         run_generic<MATH, R>(s_code, s_tile, T, P, tid, tmp, a.prot);
+         run_generic<MATH, R>(prog, a.data, a.ld, base, P, tid, tmp, a.prot);
 #pragma unroll
          for (int r = 0; r < R; ++r) v[r] = tmp[r];
       } else {
@@ -415,25 +520,48 @@ cudaError_t configure_t() {
 // per thread; opset 0 = FULL, 1 = ARITH).
 template <int MATH>
 struct Launch {
-   static cudaError_t evaluate(int opset, const EvalArgs& a, int block, int grid, size_t smem, cudaStream_t s) {
+   static cudaError_t configure(int opset) {
+      static bool done[2] = {false, false};
+      if (done[opset]) return cudaSuccess;
       cudaError_t e = opset ? configure_t<MATH, kOpsetArith>() : configure_t<MATH, kOpsetFull>();
+      if (e != cudaSuccess) return e;
+      e = cudaFuncSetAttribute(opset ? eval_batch_kernel<MATH, kR, kOpsetArith> : eval_batch_kernel<MATH, kR, kOpsetFull>,
+                               cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+      if (e == cudaSuccess) done[opset] = true;
+      return e;
+   }
+   static cudaError_t evaluate(int opset, const EvalArgs& a, int block, int grid, size_t smem, cudaStream_t s) {
+      cudaError_t e = configure(opset);
       if (e != cudaSuccess) return e;
       if (opset) eval_kernel<MATH, kR, kOpsetArith><<<grid, block, smem, s>>>(a);
       else eval_kernel<MATH, kR, kOpsetFull><<<grid, block, smem, s>>>(a);
       return cudaGetLastError();
    }
+   static cudaError_t evaluate_batch(int opset, const BatchArgs& a, int block, int grid, size_t smem, cudaStream_t s) {
+      cudaError_t e = configure(opset);
+      if (e != cudaSuccess) return e;
+      if (opset) eval_batch_kernel<MATH, kR, kOpsetArith><<<grid, block, smem, s>>>(a);
+      else eval_batch_kernel<MATH, kR, kOpsetFull><<<grid, block, smem, s>>>(a);
+      return cudaGetLastError();
+   }
    static cudaError_t predict(int opset, const PredictArgs& a, int block, int grid, size_t smem, cudaStream_t s) {
-      cudaError_t e = opset ? configure_t<MATH, kOpsetArith>() : configure_t<MATH, kOpsetFull>();
+      cudaError_t e = configure(opset);
       if (e != cudaSuccess) return e;
       if (opset) predict_kernel<MATH, kR, kOpsetArith><<<grid, block, smem, s>>>(a);
       else predict_kernel<MATH, kR, kOpsetFull><<<grid, block, smem, s>>>(a);
       return cudaGetLastError();
    }
    static cudaError_t occupancy(int opset, int block, size_t smem, int* per_sm) {
-      cudaError_t e = opset ? configure_t<MATH, kOpsetArith>() : configure_t<MATH, kOpsetFull>();
+      cudaError_t e = configure(opset);
       if (e != cudaSuccess) return e;
       if (opset) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, eval_kernel<MATH, kR, kOpsetArith>, block, smem);
       return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, eval_kernel<MATH, kR, kOpsetFull>, block, smem);
+   }
+   static cudaError_t occupancy_batch(int opset, int block, size_t smem, int* per_sm) {
+      cudaError_t e = configure(opset);
+      if (e != cudaSuccess) return e;
+      if (opset) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, eval_batch_kernel<MATH, kR, kOpsetArith>, block, smem);
+      return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, eval_batch_kernel<MATH, kR, kOpsetFull>, block, smem);
    }
 };
 

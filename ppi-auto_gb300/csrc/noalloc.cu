@@ -105,14 +105,16 @@ extern "C" ppi_status ppi_gpu_evaluate_noalloc(const ppi_gpu_config* c, const fl
 
    // Scratch layout and its size limit.
    const int code_stride = 2 * c->max_size + 2;
-   const size_t off_entries = 256;
+   const size_t off_stats = 256;
+   const size_t off_entries = align256(off_stats + sizeof(DevStats));
    const size_t off_lut = align256(off_entries + (size_t)c->n_symbols * sizeof(ppi_symbol_entry));
    const size_t off_cost = align256(off_lut + (size_t)lut_len * sizeof(int2));
    const size_t cost_elems = c->error_fn == PPI_EF_COST ? (size_t)c->cost_n * c->cost_n : 0;
    const size_t off_meta = align256(off_cost + cost_elems * sizeof(float));
    const size_t off_code = align256(off_meta + (size_t)n * sizeof(int2));
    const size_t off_work = align256(off_code + (size_t)n * code_stride * sizeof(uint2));
-   const size_t total = align256(off_work + (size_t)n * 2 * c->max_size * sizeof(uint2));
+   const size_t off_wide = align256(off_work + (size_t)n * 2 * c->max_size * sizeof(uint2));
+   const size_t total = align256(off_wide + (size_t)n * sizeof(int));
    if (total > kNoAllocScratchBytes || lut_len > (1 << 22)) {
       std::fprintf(stderr,
                    "ppi_gpu_evaluate_noalloc: %d programs of max_size %d need %zu bytes of scratch; "
@@ -135,14 +137,15 @@ extern "C" ppi_status ppi_gpu_evaluate_noalloc(const ppi_gpu_config* c, const fl
    ppi_status st = scratch_base(c->device, &base);
    if (st != PPI_OK) return st;
    auto* key = reinterpret_cast<unsigned long long*>(base);
-   auto* counters = reinterpret_cast<unsigned*>(base + 8);
-   auto* status = reinterpret_cast<int*>(base + 16);
+   auto* status = reinterpret_cast<int*>(base + 8);
+   auto* stats = reinterpret_cast<DevStats*>(base + off_stats);
    auto* entries = reinterpret_cast<ppi_symbol_entry*>(base + off_entries);
    auto* lut = reinterpret_cast<int2*>(base + off_lut);
    auto* cost = reinterpret_cast<float*>(base + off_cost);
    auto* meta = reinterpret_cast<int2*>(base + off_meta);
    auto* code = reinterpret_cast<uint2*>(base + off_code);
    auto* work = reinterpret_cast<uint2*>(base + off_work);
+   auto* wide = reinterpret_cast<int*>(base + off_wide);
 
    if (c->n_symbols > 0) {
       if (cudaMemcpyAsync(entries, c->symbols, (size_t)c->n_symbols * sizeof(ppi_symbol_entry),
@@ -157,17 +160,26 @@ extern "C" ppi_status ppi_gpu_evaluate_noalloc(const ppi_gpu_config* c, const fl
 
    TranslateArgs t{};
    t.phenotype = d_phenotype; t.ephemeral = d_ephemeral; t.size = d_size; t.n = n;
-   t.max_size = c->max_size; t.ncol = ncol; t.lut = lut; t.lut_min = mn; t.lut_len = lut_len;
+   t.max_size = c->max_size; t.ncol = ncol; t.nlin = nlin; t.lut = lut; t.lut_min = mn; t.lut_len = lut_len;
    t.code = code; t.code_stride = code_stride; t.meta = meta; t.work = work;
-   t.best_key = key; t.counters = counters; t.status = status;
+   t.best_key = key; t.stats = stats; t.status = status;
    t.prot = c->protected_fns ? 1 : 0; t.fold = 1;
+   t.rows_main = g.rows; t.rows_wide = g.rows_wide; t.wide_list = wide;
    EvalArgs e{};
    e.data = d_data; e.nlin = nlin; e.ncol = ncol; e.ld = ld; e.code = code;
    e.code_stride = code_stride; e.meta = meta; e.size = d_size; e.n = n; e.alpha = alpha;
    e.ef = c->error_fn; e.reduce_max = c->reduce_max ? 1 : 0; e.prot = c->protected_fns ? 1 : 0;
    e.cost = cost; e.cost_n = c->cost_n; e.strategy = c->strategy; e.lanes = g.lanes; e.fitness = d_fitness;
-   e.best_key = key; e.counters = counters; e.best_index = d_best_index; e.status = status;
+   e.best_key = key; e.stats = stats; e.best_index = d_best_index; e.status = status;
+   e.wide_list = wide;
+   if (cudaMemsetAsync(stats, 0, sizeof(DevStats), s) != cudaSuccess) return PPI_ERR_CUDA;
    if (launch_translate(c->math, t, s) != cudaSuccess) return PPI_ERR_CUDA;
+   e.rows = g.rows; e.wide_pass = 0; e.final_pass = g.wide ? 0 : 1;
    if (launch_evaluate(c->math, g.opset, e, g.block, g.grid, g.smem, s) != cudaSuccess) return PPI_ERR_CUDA;
+   if (g.wide) {
+      e.rows = g.rows_wide; e.wide_pass = 1; e.final_pass = 1;
+      if (launch_evaluate(c->math, g.opset, e, g.block, g.grid_wide, g.smem_wide, s) != cudaSuccess)
+         return PPI_ERR_CUDA;
+   }
    return PPI_OK;
 }

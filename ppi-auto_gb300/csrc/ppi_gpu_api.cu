@@ -45,7 +45,8 @@ struct ppi_gpu {
    uint2* d_work = nullptr;
    float* d_fit = nullptr;
    unsigned long long* d_key = nullptr;
-   unsigned* d_counters = nullptr;
+   DevStats* d_stats = nullptr;
+   int* d_wide = nullptr;
    int32_t* d_best = nullptr;
    int* d_status = nullptr;
    float* d_pred = nullptr;
@@ -53,6 +54,8 @@ struct ppi_gpu {
    float* h_fit = nullptr;
    int32_t* h_best = nullptr;
    int* h_status = nullptr;
+   unsigned long long* h_rows = nullptr;   // row histogram of the last evaluation
+   int rows_hint = 0;                      // main-pass row budget asked of plan_geometry
    // pending split call
    bool pending = false;
    int pending_n = 0;
@@ -94,10 +97,10 @@ void free_all(ppi_gpu* h) {
    cudaFree(h->d_lut); cudaFree(h->d_cost); cudaFree(h->d_data);
    cudaFree(h->d_ph); cudaFree(h->d_eph); cudaFree(h->d_size); cudaFree(h->d_code);
    cudaFree(h->d_meta); cudaFree(h->d_work); cudaFree(h->d_fit); cudaFree(h->d_key);
-   cudaFree(h->d_counters); cudaFree(h->d_best); cudaFree(h->d_status); cudaFree(h->d_pred);
+   cudaFree(h->d_stats); cudaFree(h->d_wide); cudaFree(h->d_best); cudaFree(h->d_status); cudaFree(h->d_pred);
    cudaFree(h->d_genomes); cudaFree(h->d_frames);
    free_decode_tables(&h->dec);
-   cudaFreeHost(h->h_fit); cudaFreeHost(h->h_best); cudaFreeHost(h->h_status);
+   cudaFreeHost(h->h_fit); cudaFreeHost(h->h_best); cudaFreeHost(h->h_status); cudaFreeHost(h->h_rows);
    if (h->ev0) cudaEventDestroy(h->ev0);
    if (h->ev1) cudaEventDestroy(h->ev1);
    if (h->evm) cudaEventDestroy(h->evm);
@@ -108,10 +111,21 @@ void free_all(ppi_gpu* h) {
 ppi_status plan(ppi_gpu* h) {
    Geometry g;
    const char* why = plan_geometry(h->cfg.strategy, h->lanes, h->cfg.math, h->opset, h->nlin,
-                                   h->ncol, h->code_stride, h->cfg.population_size, h->sm_count, &g);
+                                   h->ncol, h->code_stride, h->cfg.population_size, h->sm_count, &g,
+                                   h->rows_hint);
    if (why) return fail(h, PPI_ERR_UNSUPPORTED, why);
    h->geo = g;
    return PPI_OK;
+}
+
+// The next generation's programs resemble this one's: size the main pass's
+// rows to cover all but 1% of the work of the evaluation just read back
+// (h_rows).  Changes speed only, never a result.
+ppi_status update_rows_hint(ppi_gpu* h) {
+   const int hint = rows_for_histogram(h->h_rows, h->geo.rows_wide, 0.01);
+   if (hint == h->rows_hint) return PPI_OK;
+   h->rows_hint = hint;
+   return plan(h);
 }
 
 ppi_status check_ready(ppi_gpu* h, int n) {
@@ -125,27 +139,37 @@ ppi_status check_ready(ppi_gpu* h, int n) {
 
 ppi_status enqueue(ppi_gpu* h, const int32_t* d_ph, const float* d_eph, const int32_t* d_size,
                    int n, float alpha, float* d_fit, int32_t* d_best, cudaStream_t s) {
+   const Geometry& g = h->geo;
    TranslateArgs t{};
    t.phenotype = d_ph; t.ephemeral = d_eph; t.size = d_size; t.n = n;
-   t.max_size = h->cfg.max_size; t.ncol = h->ncol;
+   t.max_size = h->cfg.max_size; t.ncol = h->ncol; t.nlin = h->nlin;
    t.lut = h->d_lut; t.lut_min = h->lut_min; t.lut_len = h->lut_len;
    t.code = h->d_code; t.code_stride = h->code_stride; t.meta = h->d_meta; t.work = h->d_work;
-   t.best_key = h->d_key; t.counters = h->d_counters; t.status = h->d_status;
+   t.best_key = h->d_key; t.stats = h->d_stats; t.status = h->d_status;
    t.prot = h->cfg.protected_fns ? 1 : 0; t.fold = 1;
+   t.rows_main = g.rows; t.rows_wide = g.rows_wide; t.wide_list = h->d_wide;
    EvalArgs e{};
    e.data = h->d_data; e.nlin = h->nlin; e.ncol = h->ncol; e.ld = h->ld;
    e.code = h->d_code; e.code_stride = h->code_stride; e.meta = h->d_meta; e.size = d_size;
    e.n = n; e.alpha = alpha; e.ef = h->cfg.error_fn; e.reduce_max = h->cfg.reduce_max ? 1 : 0;
    e.prot = h->cfg.protected_fns ? 1 : 0; e.cost = h->d_cost; e.cost_n = h->cfg.cost_n;
    e.strategy = h->cfg.strategy; e.lanes = h->lanes; e.fitness = d_fit; e.best_key = h->d_key;
-   e.counters = h->d_counters; e.best_index = d_best; e.status = h->d_status;
+   e.stats = h->d_stats; e.best_index = d_best; e.status = h->d_status;
+   e.wide_list = h->d_wide;
    PPI_CUDA(h, cudaEventRecord(h->ev0, s));
+   PPI_CUDA(h, cudaMemsetAsync(h->d_stats, 0, sizeof(DevStats), s));
    PPI_CUDA(h, launch_translate(h->cfg.math, t, s));
    PPI_CUDA(h, cudaEventRecord(h->evm, s));
-   PPI_CUDA(h, launch_evaluate(h->cfg.math, h->geo.opset, e, h->geo.block, std::min(h->geo.grid, n),
-                               h->geo.smem, s));
-   PPI_CUDA(h, cudaEventRecord(h->ev1, s));
+   e.rows = g.rows; e.wide_pass = 0; e.final_pass = g.wide ? 0 : 1;
+   PPI_CUDA(h, launch_evaluate(h->cfg.math, g.opset, e, g.block, std::min(g.grid, n), g.smem, s));
    h->last_launches = 2;
+   if (g.wide) {
+      e.rows = g.rows_wide; e.wide_pass = 1; e.final_pass = 1;
+      PPI_CUDA(h, launch_evaluate(h->cfg.math, g.opset, e, g.block, std::min(g.grid_wide, n),
+                                  g.smem_wide, s));
+      h->last_launches = 3;
+   }
+   PPI_CUDA(h, cudaEventRecord(h->ev1, s));
    return PPI_OK;
 }
 
@@ -207,8 +231,9 @@ ppi_status ppi_gpu_create(const ppi_gpu_config* c, ppi_gpu** out) {
        dalloc(&h->d_code, pop * (size_t)h->code_stride) != cudaSuccess ||
        dalloc(&h->d_meta, pop) != cudaSuccess || dalloc(&h->d_work, pop * 2 * ms) != cudaSuccess ||
        dalloc(&h->d_fit, pop) != cudaSuccess || dalloc(&h->d_key, 1) != cudaSuccess ||
-       dalloc(&h->d_counters, 2) != cudaSuccess || dalloc(&h->d_best, 1) != cudaSuccess ||
-       dalloc(&h->d_status, 1) != cudaSuccess ||
+       dalloc(&h->d_stats, 1) != cudaSuccess || dalloc(&h->d_wide, pop) != cudaSuccess ||
+       dalloc(&h->d_best, 1) != cudaSuccess || dalloc(&h->d_status, 1) != cudaSuccess ||
+       cudaMallocHost(reinterpret_cast<void**>(&h->h_rows), kRowBins * sizeof(unsigned long long)) != cudaSuccess ||
        cudaMallocHost(reinterpret_cast<void**>(&h->h_fit), pop * sizeof(float)) != cudaSuccess ||
        cudaMallocHost(reinterpret_cast<void**>(&h->h_best), sizeof(int32_t)) != cudaSuccess ||
        cudaMallocHost(reinterpret_cast<void**>(&h->h_status), sizeof(int)) != cudaSuccess)
@@ -268,6 +293,7 @@ ppi_status ppi_gpu_set_dataset(ppi_gpu* h, const float* const* rows, int32_t nli
    const int L = resolve_lanes(h->cfg.strategy, h->cfg.lanes, nlin, h->sm_count);
    if (L < 1 || L > kMaxLanes) return fail(h, PPI_ERR_UNSUPPORTED, "lane count out of range");
    h->lanes = L;
+   h->rows_hint = 0;
    ppi_status s = plan(h);
    if (s != PPI_OK) return s;
    h->have_data = true;
@@ -290,6 +316,8 @@ ppi_status ppi_gpu_evaluate_launch(ppi_gpu* h, const int32_t* ph, const float* e
    PPI_CUDA(h, cudaMemcpyAsync(h->h_fit, h->d_fit, (size_t)n * 4, cudaMemcpyDeviceToHost, h->stream));
    PPI_CUDA(h, cudaMemcpyAsync(h->h_best, h->d_best, 4, cudaMemcpyDeviceToHost, h->stream));
    PPI_CUDA(h, cudaMemcpyAsync(h->h_status, h->d_status, 4, cudaMemcpyDeviceToHost, h->stream));
+   PPI_CUDA(h, cudaMemcpyAsync(h->h_rows, h->d_stats->rows_work, kRowBins * sizeof(unsigned long long),
+                               cudaMemcpyDeviceToHost, h->stream));
    h->pending = true;
    h->pending_n = n;
    h->out_fit = fitness;
@@ -305,6 +333,8 @@ ppi_status ppi_gpu_evaluate_wait(ppi_gpu* h) {
    std::memcpy(h->out_fit, h->h_fit, (size_t)h->pending_n * sizeof(float));
    if (h->out_best) *h->out_best = *h->h_best;
    cudaEventElapsedTime(&h->last_ms, h->ev0, h->ev1);
+   ppi_status s = update_rows_hint(h);
+   if (s != PPI_OK) return s;
    if (*h->h_status & kStatusUnsupportedProgram)
       return fail(h, PPI_ERR_UNSUPPORTED,
                   "a malformed program needs a deeper stack than the generic interpreter's");
@@ -342,27 +372,30 @@ ppi_status ppi_gpu_predict(ppi_gpu* h, const int32_t* ph, const float* eph, int3
       PPI_CUDA(h, cudaMemcpyAsync(h->d_eph, eph, (size_t)size * 4, cudaMemcpyHostToDevice, h->stream));
    }
    PPI_CUDA(h, cudaMemcpyAsync(h->d_size, &size, 4, cudaMemcpyHostToDevice, h->stream));
+   // one program: a tile with every row it can need (up to 200 KB; a
+   // program needing more takes the generic form)
+   const int R = kR;
+   int P = 128;
+   int rows = max_program_rows(h->ncol);
+   while (P > 32 && evaluate_smem_bytes(h->code_stride, kSlots + 2, P, R, 0, true) > 200 * 1024) P /= 2;
+   while (rows > 1 && evaluate_smem_bytes(h->code_stride, rows, P, R, 0, true) > 200 * 1024) --rows;
+   const size_t smem = evaluate_smem_bytes(h->code_stride, rows, P, R, 0, true);
+   if (smem > 200 * 1024) return fail(h, PPI_ERR_UNSUPPORTED, "program code too long for shared memory");
    TranslateArgs t{};
    t.phenotype = h->d_ph; t.ephemeral = h->d_eph; t.size = h->d_size; t.n = 1;
-   t.max_size = h->cfg.max_size; t.ncol = h->ncol;
+   t.max_size = h->cfg.max_size; t.ncol = h->ncol; t.nlin = h->nlin;
    t.lut = h->d_lut; t.lut_min = h->lut_min; t.lut_len = h->lut_len;
    t.code = h->d_code; t.code_stride = h->code_stride; t.meta = h->d_meta; t.work = h->d_work;
-   t.best_key = h->d_key; t.counters = h->d_counters; t.status = h->d_status;
+   t.best_key = h->d_key; t.stats = h->d_stats; t.status = h->d_status;
    t.prot = h->cfg.protected_fns ? 1 : 0; t.fold = 1;
+   t.rows_main = rows; t.rows_wide = rows; t.wide_list = h->d_wide;
    PredictArgs p{};
    p.data = h->d_data; p.nlin = h->nlin; p.ncol = h->ncol; p.ld = h->ld;
    p.code = h->d_code; p.meta = h->d_meta; p.prot = h->cfg.protected_fns ? 1 : 0; p.out = h->d_pred;
-   const int R = 8;
-   int P = 128;
-   size_t smem = evaluate_smem_bytes(h->code_stride, h->ncol, P, R, 0, false);
-   while (smem > 200 * 1024 && P > 32) {
-      P /= 2;
-      smem = evaluate_smem_bytes(h->code_stride, h->ncol, P, R, 0, false);
-   }
-   if (smem > 200 * 1024) return fail(h, PPI_ERR_UNSUPPORTED, "too many columns");
    const int tiles = (h->nlin + P * R - 1) / (P * R);
    const int grid = std::max(1, std::min(tiles, 4 * h->sm_count));
    PPI_CUDA(h, cudaEventRecord(h->ev0, h->stream));
+   PPI_CUDA(h, cudaMemsetAsync(h->d_stats, 0, sizeof(DevStats), h->stream));
    PPI_CUDA(h, launch_translate(h->cfg.math, t, h->stream));
    PPI_CUDA(h, launch_predict(h->cfg.math, h->opset, p, P, grid, smem, h->stream));
    PPI_CUDA(h, cudaEventRecord(h->ev1, h->stream));
@@ -487,7 +520,9 @@ ppi_status ppi_gpu_decode_evaluate(ppi_gpu* h, const uint8_t* genomes, int32_t n
    PPI_CUDA(h, launch_decode(d, h->stream));
    s = enqueue(h, h->d_ph, h->d_eph, h->d_size, n, alpha, h->d_fit, h->d_best, h->stream);
    if (s != PPI_OK) return s;
-   h->last_launches = 3;
+   h->last_launches += 1;
+   PPI_CUDA(h, cudaMemcpyAsync(h->h_rows, h->d_stats->rows_work, kRowBins * sizeof(unsigned long long),
+                               cudaMemcpyDeviceToHost, h->stream));
    PPI_CUDA(h, cudaMemcpyAsync(h->h_fit, h->d_fit, (size_t)n * 4, cudaMemcpyDeviceToHost, h->stream));
    PPI_CUDA(h, cudaMemcpyAsync(h->h_best, h->d_best, 4, cudaMemcpyDeviceToHost, h->stream));
    PPI_CUDA(h, cudaMemcpyAsync(h->h_status, h->d_status, 4, cudaMemcpyDeviceToHost, h->stream));
@@ -497,6 +532,8 @@ ppi_status ppi_gpu_decode_evaluate(ppi_gpu* h, const uint8_t* genomes, int32_t n
    std::memcpy(fitness, h->h_fit, (size_t)n * sizeof(float));
    if (best_index) *best_index = *h->h_best;
    cudaEventElapsedTime(&h->last_ms, h->ev0, h->ev1);
+   s = update_rows_hint(h);
+   if (s != PPI_OK) return s;
    if (*h->h_status & kStatusUnsupportedProgram)
       return fail(h, PPI_ERR_UNSUPPORTED, "a program needs a deeper stack than supported");
    return PPI_OK;

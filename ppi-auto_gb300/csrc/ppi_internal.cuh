@@ -18,6 +18,8 @@ constexpr int kR = 8;
 // most kSlots runs on the bytecode path.  Every binary tree of at most 255
 // nodes fits in 6 slots.
 constexpr int kSlots = 6;
+// Row-count histogram bins of the translator's statistics.
+constexpr int kRowBins = 64;
 // Largest lane count (PDP work-items per program, DP records per group).
 constexpr int kMaxLanes = 4096;
 // Stack depth of the generic (stack) interpreter used for malformed programs
@@ -29,8 +31,31 @@ constexpr int kColumnPad = 1024;
 // Opcode sets of the evaluator's bytecode path (evaluate_impl.cuh).
 enum : int { kOpsetFull = 0, kOpsetArith = 1 };
 
-// Program kinds written by the translator.
-enum : int { kKindInvalid = 0, kKindFast = 1, kKindGeneric = 2, kKindUnsupported = 3 };
+// Program kinds written by the translator.  meta.x = kind | rows << 8, where
+// rows is the number of shared-memory rows the program's tile needs; meta.y is
+// the length of its code (header included).  kKindWide: bytecode path, but
+// more rows than the main pass's budget, so it runs in the wide pass.
+enum : int { kKindInvalid = 0, kKindFast = 1, kKindGeneric = 2, kKindUnsupported = 3, kKindWide = 4 };
+__host__ __device__ __forceinline__ int meta_kind(int2 m) { return m.x & 0xFF; }
+__host__ __device__ __forceinline__ int meta_rows(int2 m) { return m.x >> 8; }
+
+// Code of one program: entry 0 is the header {k, s}: the program reads k
+// distinct record columns and needs s slot rows.  Entries 1 .. (k+1)/2 list
+// the columns, two per entry (.x, .y), in the order of their tile rows.  The
+// instructions follow.  Tile rows: 0 .. s-1 slots, s .. s+k-1 the listed
+// columns, s+k the target column (the last column of the dataset).  The
+// generic form has k = s = 0 (its attribute reads go to global memory) and
+// its tokens follow the header.
+__host__ __device__ __forceinline__ int code_header(int k) { return 1 + (k + 1) / 2; }
+
+// Translator statistics, zeroed before every translation.
+struct DevStats {
+   unsigned queue;           // work queue of the main pass
+   unsigned finished;        // CTAs finished in the final pass
+   unsigned wide;            // programs of the wide pass (plain evaluation)
+   unsigned wide_queue;      // work queue of the wide pass
+   unsigned long long rows_work[kRowBins];   // work (program size x records) by row count
+};
 
 // Status bits reported by the kernels.
 enum : int { kStatusUnsupportedProgram = 1 };
@@ -38,9 +63,9 @@ enum : int { kStatusUnsupportedProgram = 1 };
 // Accumulator-machine instructions.  Each is a uint2: .x = instruction id
 // below, .y = immediate: float bits of a constant, or a row index.
 // The only register state is `acc` (kR record values per thread).  Every
-// other operand is a "row" of the CTA's shared-memory tile: rows 0..ncol-1
-// hold the staged record columns, rows ncol..ncol+kSlots-1 are the slots
-// where a pending subexpression is parked.  Each thread reads and writes only
+// other operand is a "row" of the CTA's shared-memory tile (see
+// code_header): slots where a pending subexpression is parked, and the
+// staged record columns the program reads.  Each thread reads and writes only
 // its own kR positions of a row.
 enum : uint32_t {
    M_END = 0,
@@ -240,22 +265,41 @@ __device__ __forceinline__ float apply_error(int ef, float x, float y, const flo
 __device__ __forceinline__ bool nonfinite(float v) { return isinf(v) || isnan(v); }
 
 // ---------------------------------------------------------------------------
+// One population of a batch (device memory).
+struct PopDesc {
+   const float* data;          // column-major, column c at data + c * ld
+   int nlin, ncol, ld;
+   int strategy, lanes, ef, reduce_max, prot, cost_n;
+   const float* cost;
+   float alpha;
+   int prog_begin;             // first program of the population in the flat arrays
+   int n;                      // programs
+};
+
 struct TranslateArgs {
    const int32_t* phenotype;   // program i at phenotype + i * max_size
    const float* ephemeral;
    const int32_t* size;
-   int n, max_size, ncol;
+   int n, max_size, ncol, nlin;
    const int2* lut;            // lut[sym - lut_min] = {op, literal bits}
    int lut_min, lut_len;
    uint2* code;                // program i at code + i * code_stride
    int code_stride;
-   int2* meta;                 // {kind, code length}
+   int2* meta;                 // {kind | rows << 8, code length}
    uint2* work;                // translator scratch: n x max_size
    unsigned long long* best_key;
-   unsigned* counters;         // [0] work queue, [1] finished blocks
+   DevStats* stats;
    int* status;
    int prot;                   // PROTECTED, for constant folding
    int fold;                   // fold constant subexpressions
+   int rows_main;              // row budget of the main pass
+   int rows_wide;              // row budget of the wide pass (more rows: generic form)
+   int* wide_list;             // plain evaluation: programs of the wide pass
+   // batches: per-program population (nullptr for one population)
+   const int* pop_of;
+   const PopDesc* pops;
+   unsigned* bucket_count;     // cost buckets of the work order: [0, 64) main pass, [64, 128) wide
+   unsigned char* bucket_of;   // bucket of each program
 };
 
 struct EvalArgs {
@@ -273,9 +317,33 @@ struct EvalArgs {
    int strategy, lanes;
    float* fitness;
    unsigned long long* best_key;
-   unsigned* counters;
+   DevStats* stats;
    int32_t* best_index;
    int* status;
+   int rows;                   // row budget of this pass's tile
+   int wide_pass;              // 0: main pass (skips kKindWide), 1: programs of wide_list
+   const int* wide_list;
+   int final_pass;             // this pass writes the best index
+};
+
+struct BatchArgs {
+   const PopDesc* pops;
+   const int* pop_of;          // population of each program
+   const int* order;           // work items: program indices, largest cost first
+   int total;
+   const uint2* code;
+   int code_stride;
+   const int2* meta;
+   const int32_t* size;
+   float* fitness;             // flat, all populations
+   unsigned long long* pop_key;
+   unsigned* pop_done;
+   int32_t* best_index;        // one per population
+   DevStats* stats;
+   const unsigned* n_main;     // order[0, *n_main): main pass; the rest: wide pass
+   int* status;
+   int rows;                   // row budget of this pass's tile
+   int wide_pass;
 };
 
 struct PredictArgs {
@@ -287,18 +355,33 @@ struct PredictArgs {
    float* out;
 };
 
-// Evaluator launch geometry: lanes, block size P, records per thread R,
-// dynamic shared memory and a one-wave persistent grid.
+// Evaluator launch geometry: lanes, block size P, records per thread R, and
+// for the main and the wide pass the row budget, dynamic shared memory and a
+// one-wave persistent grid.  wide == false when no program can need more
+// rows than the main pass has (the wide pass is not launched).
 struct Geometry {
-   int lanes = 1, block = 128, R = 8, grid = 1, opset = kOpsetFull;
+   int lanes = 1, block = 128, R = 8, opset = kOpsetFull;
+   int rows = 1, grid = 1;
    size_t smem = 0;
+   int rows_wide = 1, grid_wide = 1;
+   size_t smem_wide = 0;
+   bool wide = false;
+   bool aligned = false;
+   int per_sm[2] = {0, 0};     // resident CTAs per SM of the two passes
 };
 // kOpsetArith when every op of the symbol table is in the ARITH set.
 int opset_for(const ppi_symbol_entry* symbols, int n);
 int resolve_lanes(int strategy, int lanes, int nlin, int sm_count);
 // Returns nullptr on success, else why the configuration is unsupported.
+// rows_hint > 0 asks for that main-pass row budget (clamped to what fits);
+// 0 takes the largest budget at full occupancy.
 const char* plan_geometry(int strategy, int lanes, int math, int opset, int nlin, int ncol,
-                          int code_stride, int n_max, int sm_count, Geometry* g);
+                          int code_stride, int n_max, int sm_count, Geometry* g, int rows_hint = 0);
+// Main-pass row budget for the work histogram of a previous translation:
+// the smallest budget that covers all but `spill` of the work.
+int rows_for_histogram(const unsigned long long* rows_work, int rows_cap, double spill);
+// Largest program row count on a dataset of ncol columns.
+inline int max_program_rows(int ncol) { return kSlots + ncol + 1; }
 
 // Kernel launchers (evaluate.cu / translate.cu).
 cudaError_t launch_translate(int math, const TranslateArgs& a, cudaStream_t s);
@@ -306,7 +389,13 @@ cudaError_t launch_evaluate(int math, int opset, const EvalArgs& a, int block, i
                             cudaStream_t s);
 cudaError_t launch_predict(int math, int opset, const PredictArgs& a, int block, int grid, size_t smem,
                            cudaStream_t s);
+cudaError_t launch_evaluate_batch(int math, int opset, const BatchArgs& a, int block, int grid,
+                                  size_t smem, cudaStream_t s);
+cudaError_t launch_batch_order(const unsigned* bucket_count, unsigned* cursor,
+                               const unsigned char* bucket_of, int* order, int total,
+                               unsigned* n_main, cudaStream_t s);
 cudaError_t evaluate_occupancy(int math, int opset, int block, size_t smem, int* blocks_per_sm);
-size_t evaluate_smem_bytes(int code_stride, int ncol, int block, int R, int lanes, bool aligned);
+cudaError_t evaluate_batch_occupancy(int math, int opset, int block, size_t smem, int* blocks_per_sm);
+size_t evaluate_smem_bytes(int code_stride, int rows, int block, int R, int lanes, bool aligned);
 
 }  // namespace ppi

@@ -21,6 +21,12 @@
 // programs needing more than kSlots registers get the generic form instead:
 // the mapped tokens in evaluation order, run by a stack interpreter with the
 // reference's stack semantics.
+// Between the passes the distinct record columns the program reads (after
+// folding) are listed in the code header and given tile rows after the slot
+// rows, so the evaluator stages only those columns (and the target).  A
+// program's tile row count decides its pass: the main pass (rows within the
+// launch's main budget), the wide pass (within the wide budget), or the
+// generic form.
 #include "ppi_internal.cuh"
 
 namespace ppi {
@@ -89,26 +95,14 @@ __device__ float fold(int op, float x0, float x1, float x2, int prot) {
 
 __device__ __forceinline__ bool is_const_leaf(int op) { return op == PPI_OP_CONST || op == PPI_OP_LITERAL; }
 
+// Translation of program i (valid size): writes its code, returns its meta.
 template <int MATH>
-__global__ void translate_kernel(const TranslateArgs a) {
-   if (blockIdx.x == 0 && threadIdx.x == 0) {
-      *a.best_key = ~0ull;
-      a.counters[0] = 0u;
-      a.counters[1] = 0u;
-      *a.status = 0;
-   }
-   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-   if (i >= a.n) return;
-   const int sz = a.size[i];
-   if (sz <= 0 || sz > a.max_size) {
-      a.meta[i] = make_int2(kKindInvalid, 0);
-      return;
-   }
-   const int32_t* ph = a.phenotype + (size_t)i * a.max_size;
-   const float* eph = a.ephemeral + (size_t)i * a.max_size;
-   uint2* w = a.work + (size_t)i * 2 * a.max_size;
-   uint32_t* frames = reinterpret_cast<uint32_t*>(w + a.max_size);
-   uint2* code = a.code + (size_t)i * a.code_stride;
+__device__ int2 translate_program(const TranslateArgs& ta, int i, int sz) {
+   const int32_t* ph = ta.phenotype + (size_t)i * ta.max_size;
+   const float* eph = ta.ephemeral + (size_t)i * ta.max_size;
+   uint2* w = ta.work + (size_t)i * 2 * ta.max_size;
+   uint32_t* frames = reinterpret_cast<uint32_t*>(w + ta.max_size);
+   uint2* code = ta.code + (size_t)i * ta.code_stride;
 
    // ---- pass 1 -----------------------------------------------------------
    int depth = 0, stack_need = 0;
@@ -116,14 +110,14 @@ __global__ void translate_kernel(const TranslateArgs a) {
    for (int k = sz - 1; k >= 0; --k) {
       int op;
       uint32_t imm;
-      map_token(a, ph[k], eph[k], &op, &imm);
+      map_token(ta, ph[k], eph[k], &op, &imm);
       const int ar = op_arity(op);
       int before = depth;
       if (before < ar) { malformed = true; before = ar; }   // missing operands read as NaN
       depth = before - ar + 1;
       stack_need = max(stack_need, max(before, depth));
       int need = 0, sub = 1;
-      if (!malformed && ar > 0 && a.fold) {
+      if (!malformed && ar > 0 && ta.fold) {
          // children: c0 = k+1, c1 after c0's subtree, c2 after c1's
          const int c0 = k + 1;
          const int c1 = ar > 1 ? c0 + node_sub(w[c0]) : c0;
@@ -133,7 +127,7 @@ __global__ void translate_kernel(const TranslateArgs a) {
          if (ar > 2) all_const = all_const && is_const_leaf(node_op(w[c2]));
          if (all_const) {
             const float v = fold<MATH>(op, __uint_as_float(w[c0].y), __uint_as_float(w[c1].y),
-                                       __uint_as_float(w[c2].y), a.prot);
+                                       __uint_as_float(w[c2].y), ta.prot);
             int s = 1 + node_sub(w[c0]);
             if (ar > 1) s += node_sub(w[c1]);
             if (ar > 2) s += node_sub(w[c2]);
@@ -174,10 +168,36 @@ __global__ void translate_kernel(const TranslateArgs a) {
    }
    if (depth != 1) malformed = true;
 
+   // ---- columns: distinct record columns read, in order of first use ------
+   const int cap = ta.code_stride;
+   const int slots = malformed ? 0 : node_need(w[0]);
+   bool fast = !malformed && slots <= kSlots && node_sub(w[0]) == sz;
+   int ncols = 0, rows = 0;
+   if (fast) {
+      uint32_t* cols = frames + ta.max_size;   // upper half: the walk below uses at most sz frames
+      for (int p = 0; p < sz;) {
+         const uint2 wn = w[p];
+         const int op = node_op(wn);
+         if (op == PPI_OP_LITERAL) { p += node_sub(wn); continue; }   // a folded subtree is one literal
+         if (op == PPI_OP_ATTRIBUTE) {
+            int j = 0;
+            while (j < ncols && cols[j] != wn.y) ++j;
+            if (j == ncols) cols[ncols++] = wn.y;
+            w[p].y = (uint32_t)(slots + j);                // its tile row
+         }
+         ++p;
+      }
+      rows = slots + ncols + 1;
+      if (rows > ta.rows_wide || code_header(ncols) >= cap) fast = false;
+      if (fast) {
+         code[0] = make_uint2((uint32_t)ncols, (uint32_t)slots);
+         for (int j = 0; j < ncols; j += 2)
+            code[1 + j / 2] = make_uint2(cols[j], j + 1 < ncols ? cols[j + 1] : 0u);
+      }
+   }
+
    // ---- pass 2: register code ---------------------------------------------
-   const int cap = a.code_stride;
-   int ncode = 0;
-   bool fast = !malformed && node_need(w[0]) <= kSlots && node_sub(w[0]) == sz;
+   int ncode = code_header(ncols);
    if (fast) {
       int fp = 0;
       frames[fp++] = frame(0, 0, 0);
@@ -187,7 +207,7 @@ __global__ void translate_kernel(const TranslateArgs a) {
       };
       auto is_leaf = [&](int node) { return op_arity(node_op(w[node])) == 0; };
       auto leaf_attr = [&](int node) { return node_op(w[node]) == PPI_OP_ATTRIBUTE; };
-      const uint32_t slot0 = (uint32_t)a.ncol;   // row of slot 0
+      const uint32_t slot0 = 0u;   // row of slot 0
       while (fp > 0) {
          const uint32_t f = frames[fp - 1];
          const int node = (int)(f & 0xFFFFu), d = (int)((f >> 16) & 0xFFu), st = (int)(f >> 24);
@@ -270,22 +290,56 @@ __global__ void translate_kernel(const TranslateArgs a) {
       if (ncode > cap) fast = false;
    }
    if (fast) {
-      a.meta[i] = make_int2(kKindFast, ncode);
-      return;
+      const int kind = rows <= ta.rows_main ? kKindFast : kKindWide;
+      return make_int2(kind | (rows << 8), ncode);
    }
    // ---- generic form: tokens in evaluation order ---------------------------
-   if (stack_need > kGenericStack) {
-      a.meta[i] = make_int2(kKindUnsupported, 0);
-      return;
-   }
-   for (int k = sz - 1; k >= 0; --k) {   // the original tokens: nothing folded
+   if (stack_need > kGenericStack) return make_int2(kKindUnsupported, 0);
+   code[0] = make_uint2(0u, 0u);          // no staged columns, no slots: the target is row 0
+   for (int k = sz - 1; k >= 0; --k) {    // the original tokens: nothing folded
       int op;
       uint32_t imm;
-      map_token(a, ph[k], eph[k], &op, &imm);
-      code[sz - 1 - k] = make_uint2((uint32_t)op, imm);
+      map_token(ta, ph[k], eph[k], &op, &imm);
+      code[1 + sz - 1 - k] = make_uint2((uint32_t)op, imm);
    }
-   code[sz] = make_uint2(kGenericEnd, 0u);
-   a.meta[i] = make_int2(kKindGeneric, sz + 1);
+   code[1 + sz] = make_uint2(kGenericEnd, 0u);
+   return make_int2(kKindGeneric | (1 << 8), sz + 2);
+}
+
+template <int MATH>
+__global__ void translate_kernel(const TranslateArgs a) {
+   if (blockIdx.x == 0 && threadIdx.x == 0) {
+      *a.best_key = ~0ull;
+      *a.status = 0;
+   }
+   const int i = blockIdx.x * blockDim.x + threadIdx.x;
+   if (i >= a.n) return;
+   const int sz = a.size[i];
+   TranslateArgs ta = a;
+   long long nlin = a.nlin;
+   if (a.pop_of) {
+      // batch: this program's dataset width and protection
+      const PopDesc& pd = a.pops[a.pop_of[i]];
+      ta.ncol = pd.ncol;
+      ta.prot = pd.prot;
+      nlin = pd.nlin;
+   }
+   const bool valid = sz > 0 && sz <= a.max_size;   // sizes outside [1, max_size] are size 0
+   const int2 m = valid ? translate_program<MATH>(ta, i, sz) : make_int2(kKindInvalid, 0);
+   a.meta[i] = m;
+   const int kind = meta_kind(m);
+   const unsigned long long work = valid ? (unsigned long long)sz * (unsigned long long)nlin : 0ull;
+   if (valid) atomicAdd(&a.stats->rows_work[min(meta_rows(m), kRowBins - 1)], work);
+   if (a.pop_of) {
+      // work order of a batch: cost buckets (cost = size x records), largest
+      // first; the wide pass's programs in their own buckets
+      int b = work ? 64 - __clzll(work) : 0;   // 0..63
+      if (kind == kKindWide) b += 64;
+      a.bucket_of[i] = (unsigned char)b;
+      atomicAdd(&a.bucket_count[b], 1u);
+   } else if (kind == kKindWide) {
+      a.wide_list[atomicAdd(&a.stats->wide, 1u)] = i;
+   }
 }
 
 }  // namespace

@@ -46,6 +46,17 @@ class Config(C.Structure):
                 ("n_symbols", C.c_int32), ("device", C.c_int32)]
 
 
+class BatchPopulation(C.Structure):
+    _fields_ = [("rows", _fp), ("nlin", C.c_int32), ("ncol", C.c_int32), ("n", C.c_int32),
+                ("strategy", C.c_int32), ("lanes", C.c_int32), ("error_fn", C.c_int32),
+                ("reduce_max", C.c_int32), ("protected_fns", C.c_int32), ("cost", _fp),
+                ("cost_n", C.c_int32)]
+
+
+BATCH_GRAPH = 1
+BATCH_AUTOTUNE = 2
+
+
 def lib_path():
     return _build.LIB
 
@@ -87,6 +98,17 @@ def load_library():
     L.ppi_gpu_last_launch_count.argtypes = [C.c_void_p]
     L.ppi_gpu_last_stage_ms.argtypes = [C.c_void_p, _fp, _fp]
     L.ppi_gpu_lanes.argtypes = [C.c_void_p]
+    L.ppi_batch_create.argtypes = [C.POINTER(Config), C.c_int32, C.POINTER(BatchPopulation),
+                                   C.POINTER(C.c_void_p)]
+    L.ppi_batch_destroy.argtypes = [C.c_void_p]
+    L.ppi_batch_last_error.restype = C.c_char_p
+    L.ppi_batch_last_error.argtypes = [C.c_void_p]
+    L.ppi_batch_set_alpha.argtypes = [C.c_void_p, _fp]
+    L.ppi_batch_evaluate.argtypes = [C.c_void_p, _ip, _fp, _ip, _fp, _ip, C.c_int32]
+    L.ppi_batch_evaluate_device.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                            C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32]
+    L.ppi_batch_last_kernel_ms.argtypes = [C.c_void_p, _fp]
+    L.ppi_batch_shape.argtypes = [C.c_void_p, _ip, _ip, _fp]
     _lib = L
     return L
 
@@ -95,7 +117,7 @@ def exported_symbols(header=None):
     """Function names declared in include/ppi_gpu.h (for export checks)."""
     header = header or os.path.join(_build.INCLUDE, "ppi_gpu.h")
     text = open(header).read()
-    return sorted(set(re.findall(r"\b(ppi_gpu_\w+)\s*\(", text)))
+    return sorted(set(re.findall(r"\b(ppi_(?:gpu|batch)_\w+)\s*\(", text)))
 
 
 def _f(a):
@@ -231,3 +253,86 @@ class Evaluator:
 
     def last_launch_count(self):
         return int(self._L.ppi_gpu_last_launch_count(self._h))
+
+
+class BatchEvaluator:
+    """Many populations in one launch (ppi_batch_* of the C ABI).
+
+    pops: list of dicts with keys rows, n and optionally strategy, lanes,
+    error_fn, cost, reduce_max, protected.  Programs, fitness: all
+    populations concatenated in order (rows of max_size)."""
+
+    def __init__(self, symtab, max_size, pops, math="fast", device=0):
+        L = load_library()
+        sv, so, sl = symtab
+        self._syms = (SymbolEntry * max(1, len(sv)))()
+        for k in range(len(sv)):
+            self._syms[k] = SymbolEntry(int(sv[k]), int(so[k]), float(sl[k]))
+        cfg = Config(max_size, 1, 0, 0, 0, 0, 0, MATH[math], None, 0, self._syms, len(sv), device)
+        self._keep = []
+        arr = (BatchPopulation * len(pops))()
+        for i, p in enumerate(pops):
+            rows = np.ascontiguousarray(p["rows"], np.float32)
+            cost = p.get("cost")
+            cost = None if cost is None else np.ascontiguousarray(cost, np.float32)
+            self._keep += [rows, cost]
+            arr[i] = BatchPopulation(_f(rows), rows.shape[0], rows.shape[1], int(p["n"]),
+                                     STRATEGY[p.get("strategy", "PDP")], int(p.get("lanes", 0)),
+                                     ERROR_FN[p.get("error_fn", "abs")], int(p.get("reduce_max", 0)),
+                                     int(p.get("protected", 0)),
+                                     _f(cost) if cost is not None else None,
+                                     0 if cost is None else cost.shape[0])
+        h = C.c_void_p()
+        st = L.ppi_batch_create(C.byref(cfg), len(pops), arr, C.byref(h))
+        if st != 0:
+            raise PpiGpuError(st, "ppi_batch_create failed")
+        self._h, self._L = h, L
+        self.max_size = max_size
+        self.counts = [int(p["n"]) for p in pops]
+        self.total = sum(self.counts)
+
+    def _check(self, st):
+        if st != 0:
+            raise PpiGpuError(st, self._L.ppi_batch_last_error(self._h).decode())
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.ppi_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_alpha(self, alpha):
+        a = np.ascontiguousarray(alpha, np.float32)
+        self._check(self._L.ppi_batch_set_alpha(self._h, _f(a)))
+
+    def evaluate(self, phenotype, ephemeral, size, flags=0):
+        ph = np.ascontiguousarray(phenotype, np.int32)
+        ep = np.ascontiguousarray(ephemeral, np.float32)
+        sz = np.ascontiguousarray(size, np.int32)
+        assert ph.shape == (self.total, self.max_size)
+        fit = np.empty(self.total, np.float32)
+        best = np.zeros(len(self.counts), np.int32)
+        self._check(self._L.ppi_batch_evaluate(self._h, _i(ph), _f(ep), _i(sz), _f(fit), _i(best),
+                                               flags))
+        return fit, best
+
+    def evaluate_device(self, d_ph, d_eph, d_size, d_fit, d_best, stream=0, flags=0):
+        self._check(self._L.ppi_batch_evaluate_device(self._h, d_ph, d_eph, d_size, d_fit, d_best,
+                                                      stream, flags))
+
+    def last_kernel_ms(self):
+        ms = np.zeros(1, np.float32)
+        self._check(self._L.ppi_batch_last_kernel_ms(self._h, _f(ms)))
+        return float(ms[0])
+
+    def shape(self):
+        b = np.zeros(1, np.int32)
+        g = np.zeros(1, np.int32)
+        t = np.zeros(2, np.float32)
+        self._check(self._L.ppi_batch_shape(self._h, _i(b), _i(g), _f(t)))
+        return int(b[0]), int(g[0]), (float(t[0]), float(t[1]))

@@ -113,3 +113,97 @@ def streaming(seed=7, nlin=4_000_000, population=30_000, nb=4000, native=False):
 
 
 BUILDERS = {"polynomial": polynomial, "iris": iris_shaped, "stream": streaming}
+
+
+def random_programs(rng, lengths, ncol, grammar, p_unary=0.2, lo=-10.0, hi=10.0):
+    """Random valid prefix programs of the given lengths over the arithmetic
+    grammar's symbols (+ - * / and its unary ops; leaves: attributes and
+    constants).  Each program is a random sequence of node arities with one
+    more leaf than binary nodes, rotated to its unique valid start (the cycle
+    lemma), so every length gives a well-formed tree.  Returns
+    (phenotype, ephemeral) rows of max(lengths) entries."""
+    S = grammar.symbols
+    binary = [S[k] for k in ("T_ADD", "T_SUB", "T_MULT", "T_DIV") if k in S]
+    unary = [S[k] for k in ("T_SIN", "T_COS", "T_EXP", "T_LOG", "T_SQRT", "T_POW2") if k in S]
+    attr, const = S["T_ATTRIBUTE"], S["T_CONST"]
+    n = len(lengths)
+    width = int(max(lengths))
+    ph = np.zeros((n, width), np.int32)
+    ep = np.zeros((n, width), np.float32)
+    for k in np.unique(lengths):
+        idx = np.flatnonzero(lengths == k)
+        m = len(idx)
+        # node counts: u unary, b binary, b + 1 leaves, 2b + 1 + u = k
+        u = np.minimum(rng.binomial(k, p_unary, m), (k - 1))
+        odd = (k - 1 - u) % 2                # k - 1 - u must be even
+        u = np.where(u - odd >= 0, u - odd, u + odd)
+        b = (k - 1 - u) // 2
+        pos = np.arange(k)[None, :]
+        arity = np.where(pos < b[:, None], 2, np.where(pos < (b + u)[:, None], 1, 0))
+        arity = np.take_along_axis(arity, np.argsort(rng.random((m, k)), 1), 1)
+        # Read right to left, a prefix program is valid when every running
+        # sum of (1 - arity) is >= 1.  In the reversed sequence the rotation
+        # that starts right after the last minimum of the running sum is the
+        # only valid one.
+        rev = arity[:, ::-1]
+        walk = np.cumsum(1 - rev, 1)
+        last_min = k - 1 - np.argmin(walk[:, ::-1], 1)
+        rot = (last_min[:, None] + 1 + np.arange(k)[None, :]) % k
+        arity = np.take_along_axis(rev, rot, 1)[:, ::-1]
+        sym = np.where(arity == 2, rng.choice(binary, (m, k)),
+                       np.where(arity == 1, rng.choice(unary, (m, k)),
+                                np.where(rng.random((m, k)) < 0.5, attr, const)))
+        e = np.where(sym == attr, rng.integers(0, ncol, (m, k)).astype(np.float32),
+                     np.where(sym == const, rng.uniform(lo, hi, (m, k)).astype(np.float32), 0.0))
+        ph[idx, :k] = sym
+        ep[idx, :k] = e
+    return ph, ep
+
+
+def _random_target(rng, X, depth=5):
+    """A random depth-`depth` expression over the columns of X (float64)."""
+    if depth == 0:
+        return X[:, rng.integers(X.shape[1])] if rng.random() < 0.7 else np.full(len(X), rng.uniform(-2, 2))
+    op = rng.integers(6)
+    a = _random_target(rng, X, depth - 1)
+    if op == 0:
+        return np.sin(a)
+    if op == 1:
+        return np.exp(np.clip(a, -5, 5))
+    if op == 2:
+        return np.log(np.abs(a) + 1.0)
+    b = _random_target(rng, X, depth - 1)
+    if op == 3:
+        return a * b
+    if op == 4:
+        return a / (np.abs(b) + 1.0)
+    return a + b
+
+
+def uneven_batch(seed=11, n_pops=64, pop_range=(256, 30000), rec_range=(100, 1_000_000),
+                 feat_range=(1, 32), mean_len=40, len_range=(4, 256), max_size=256):
+    """Uneven batch: n_pops populations with log-uniform sizes and record
+    counts, 1-32 N(0,1) features, targets from a random depth-5 expression +
+    N(0, 0.05) noise, and programs of geometric length (mean 40, 4..256)
+    generated as random valid prefix trees.  Returns (grammar, list of
+    population dicts with rows / n / phenotype / ephemeral / size)."""
+    rng = np.random.default_rng(seed)
+    g = G.load(os.path.join(GRAMMARS, "config2_poly.bnf"))
+    pops = []
+    for p in range(n_pops):
+        n = int(np.exp(rng.uniform(np.log(pop_range[0]), np.log(pop_range[1]))))
+        nlin = int(np.exp(rng.uniform(np.log(rec_range[0]), np.log(rec_range[1]))))
+        nfeat = int(rng.integers(feat_range[0], feat_range[1] + 1))
+        X = rng.normal(0.0, 1.0, (nlin, nfeat))
+        y = _random_target(rng, X) + rng.normal(0.0, 0.05, nlin)
+        rows = np.concatenate([X, y[:, None]], 1).astype(np.float32)
+        lengths = np.clip(rng.geometric(1.0 / mean_len, n), len_range[0], len_range[1])
+        ph, ep = random_programs(rng, lengths, nfeat, g)
+        phf = np.zeros((n, max_size), np.int32)
+        epf = np.zeros((n, max_size), np.float32)
+        phf[:, :ph.shape[1]] = ph
+        epf[:, :ep.shape[1]] = ep
+        pops.append(dict(rows=rows, n=n, phenotype=phf, ephemeral=epf,
+                         size=lengths.astype(np.int32), strategy="PDP", error_fn="abs",
+                         protected=True))
+    return g, pops

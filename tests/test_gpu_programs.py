@@ -193,3 +193,39 @@ def test_constant_subexpressions_fold_exactly(gpu_lib, oracle_lib, fixture, math
         f1, _ = ev.evaluate(ph, ep, sz, 1e-6)
         f2, _ = ev.evaluate(ph, ep, sz, 1e-6)
         assert np.array_equal(f1.view(np.int32), f2.view(np.int32))
+
+
+def _sum_of_columns(gen, cols):
+    """Left-deep sum of the given attribute columns (register need 0)."""
+    G = gen.G
+    add = gen.by_op[G.OP["ADD"]][0]
+    attr = gen.by_op[G.OP["ATTRIBUTE"]][0]
+    return [(add, 0.0)] * (len(cols) - 1) + [(attr, float(c)) for c in cols]
+
+
+@pytest.mark.parametrize("strat,lanes", [("PDP", 0), ("PP", 0), ("DP", 64), ("PDP", 100)])
+def test_wide_dataset_main_wide_and_generic_tiles(gpu_lib, oracle_lib, strat, lanes):
+    """A 90-column dataset: programs reading a few columns fit the main pass's
+    tile, programs reading 20-40 distinct columns need the wide pass, and
+    ones reading 70+ columns exceed any tile and take the generic form.  The
+    second evaluation runs with the row budget re-planned from the first
+    one's histogram; both must match the oracle bit for bit."""
+    d = load_golden("allops")
+    rng = np.random.default_rng(77 + lanes)
+    rows = _dataset(rng, 3000, 90)
+    gen = ProgramGen(d, rng, rows.shape[1])
+    progs = [gen.random(int(k)) for k in rng.integers(0, 40, 60)]
+    for k in (1, 5, 12, 20, 30, 40, 55, 70, 85):
+        progs.append(_sum_of_columns(gen, rng.permutation(90)[:k]))
+        progs.append([gen.op_tok(1)] + _sum_of_columns(gen, rng.integers(0, 90, k)))   # repeats
+    rng.shuffle(progs)
+    ph, ep, sz = ProgramGen.rows(progs, 200)
+    ev = make_evaluator(d, strat, lanes, "parity", population=len(sz), max_size=200, rows=rows)
+    ref = oracle_for(oracle_lib, d, rows=rows).evaluate(ph, ep, sz, strat, ev.lanes, 1e-6)
+    for rep in range(2):
+        f, best = ev.evaluate(ph, ep, sz, 1e-6)
+        assert_bitexact(f, ref, "%s%d rep %d" % (strat, lanes, rep))
+        assert best == oracle_lib.best_index(ref)
+    pred = ev.predict(ph[-1], ep[-1], int(sz[-1]))
+    assert_bitexact(pred, oracle_for(oracle_lib, d, rows=rows).predict(ph[-1], ep[-1], int(sz[-1])),
+                    "predict")
