@@ -219,7 +219,8 @@ typedef struct {
 } ppi_batch_population;
 
 #define PPI_BATCH_GRAPH 1     /* capture the step into a CUDA graph and replay it   */
-#define PPI_BATCH_AUTOTUNE 2  /* on the first call, time each block shape, keep the fastest */
+#define PPI_BATCH_AUTOTUNE 2  /* on the first call, time the block shapes and tile row
+                                 budgets (one per occupancy level), keep the fastest */
 
 typedef struct ppi_batch ppi_batch;
 
@@ -243,9 +244,17 @@ ppi_status ppi_batch_evaluate_device(ppi_batch* b, const int32_t* d_phenotype,
                                      int32_t flags);
 /* Device time of the last step (waits for it). */
 ppi_status ppi_batch_last_kernel_ms(ppi_batch* b, float* ms);
-/* Block size and grid in use; tune_ms (may be NULL) receives the autotuner's
- * timings of the 64- and 128-thread shapes (-1: shape does not fit). */
-ppi_status ppi_batch_shape(const ppi_batch* b, int32_t* block, int32_t* grid, float* tune_ms);
+/* Block size and main-pass grid in use; rows (may be NULL) receives the tile
+ * rows of the main and the wide pass; tune_ms (may be NULL) the autotuner's
+ * timings of the 64- and 128-thread shapes at their best rows (-1: shape does
+ * not fit). */
+ppi_status ppi_batch_shape(const ppi_batch* b, int32_t* block, int32_t* grid, int32_t* rows,
+                           float* tune_ms);
+/* Fix the shape instead of tuning it: block 64 or 128 threads, and the main
+ * pass's tile rows (0: the most rows at full occupancy; clamped to what fits).
+ * Programs whose tile needs more rows run in the wide pass.  Changes speed
+ * only, never a result. */
+ppi_status ppi_batch_set_shape(ppi_batch* b, int32_t block, int32_t rows);
 
 /* No counterpart in the reference.  One generation evaluated without
  * allocating any memory, for callers that cannot allocate where they evaluate:

@@ -79,7 +79,8 @@ using namespace ppi;
 // Launch shape of the two passes.
 struct BatchGeo {
    int block = 128;
-   int rows = 1, grid = 1;
+   int rows = 1, grid = 1, per_sm = 1;
+   int fit = 1;                        // most rows any tile can have
    size_t smem = 0;
    int rows_wide = 1, grid_wide = 1;
    size_t smem_wide = 0;
@@ -117,14 +118,12 @@ struct ppi_batch {
    float* h_fit = nullptr;
    int32_t* h_best = nullptr;
    int* h_status = nullptr;
-   unsigned long long* h_rows = nullptr;
    cudaStream_t stream = nullptr;
    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
    // geometry
    BatchGeo geo;
    int max_ncol = 1, max_lanes_unaligned = 0;
    bool tuned = false;
-   int tune_blocks[2] = {64, 128};
    float tune_ms[2] = {0.0f, 0.0f};
    // graph of one step, keyed by the buffers it was captured with
    cudaGraphExec_t graph = nullptr;
@@ -161,7 +160,7 @@ void bfree_all(ppi_batch* b) {
    cudaFree(b->d_lut); cudaFree(b->d_pops); cudaFree(b->d_pop_of); cudaFree(b->d_order);
    cudaFree(b->d_bucket_of); cudaFree(b->d_bucket); cudaFree(b->d_pop_key); cudaFree(b->d_pop_done);
    cudaFree(b->d_best); cudaFree(b->d_stats); cudaFree(b->d_key); cudaFree(b->d_status);
-   cudaFree(b->d_n_main); cudaFreeHost(b->h_rows);
+   cudaFree(b->d_n_main);
    cudaFree(b->d_ph); cudaFree(b->d_eph); cudaFree(b->d_size); cudaFree(b->d_fit);
    cudaFree(b->d_code); cudaFree(b->d_meta); cudaFree(b->d_work);
    cudaFreeHost(b->h_fit); cudaFreeHost(b->h_best); cudaFreeHost(b->h_status);
@@ -170,10 +169,13 @@ void bfree_all(ppi_batch* b) {
    if (b->stream) cudaStreamDestroy(b->stream);
 }
 
-// Geometry for block size P: the main pass's rows (the most at the
-// occupancy of a one-row tile, or rows_hint when it asks for more) and the
-// wide pass's rows (every program of the widest dataset, up to 200 KB).
-ppi_status batch_geometry(ppi_batch* b, int P, int rows_hint, BatchGeo* g) {
+// Geometry for block size P.  Main pass (programs whose columns all fit, on
+// the kernel without direct reads): rows_req rows when > 0 (clamped to what
+// fits), else the most rows at the occupancy of a one-row tile.  Wide pass
+// (the rest, on the kernel with direct column reads): the most rows at its
+// own top occupancy, and at least room for the deepest slot need and the
+// target.
+ppi_status batch_geometry(ppi_batch* b, int P, int rows_req, BatchGeo* g) {
    for (const PopDesc& p : b->host_pops)
       if (p.strategy == PPI_STRATEGY_DP && p.lanes > P * kR)
          return bfail(b, PPI_ERR_UNSUPPORTED, "DP lanes larger than the tile");
@@ -188,25 +190,36 @@ ppi_status batch_geometry(ppi_batch* b, int P, int rows_hint, BatchGeo* g) {
    };
    const size_t fixed = smem_for(1) - T * 4;
    if (fixed + T * 4 > kSmemCap) return bfail(b, PPI_ERR_UNSUPPORTED, "tile does not fit in shared memory");
-   const int rows_wide = (int)std::min<size_t>(max_program_rows(b->max_ncol), (kSmemCap - fixed) / (T * 4));
-   auto occupancy = [&](int rows) {
+   const int rows_max = max_program_rows(b->max_ncol);
+   const int fit = (int)std::min<size_t>(rows_max, (kSmemCap - fixed) / (T * 4));
+   auto occupancy = [&](int direct, int rows) {
       int per_sm = 0;
-      if (evaluate_batch_occupancy(b->math, b->opset, P, smem_for(rows), &per_sm) != cudaSuccess) return 0;
+      if (evaluate_batch_occupancy(b->math, b->opset, direct, P, smem_for(rows), &per_sm) != cudaSuccess)
+         return 0;
       return per_sm;
    };
-   const int top = occupancy(1);
-   if (top < 1) return bfail(b, PPI_ERR_UNSUPPORTED, "evaluator does not fit on an SM");
-   int rows = 1;
-   while (rows < rows_wide && occupancy(rows + 1) >= top) ++rows;
-   if (rows_hint > rows) rows = std::min(rows_hint, rows_wide);
+   auto best_rows = [&](int direct) {
+      const int top = occupancy(direct, 1);
+      int rows = 1;
+      while (rows < fit && occupancy(direct, rows + 1) >= top) ++rows;
+      return rows;
+   };
+   if (occupancy(0, 1) < 1 || occupancy(1, 1) < 1)
+      return bfail(b, PPI_ERR_UNSUPPORTED, "evaluator does not fit on an SM");
+   int rows = best_rows(0);
+   if (rows_req > 0) rows = std::min(rows_req, fit);
+   const int rows2 = std::max(best_rows(1), std::min(fit, kSlots + 1));
    g->block = P;
+   g->fit = fit;
    g->rows = rows;
    g->smem = smem_for(rows);
-   g->grid = std::max(1, std::min(b->total, occupancy(rows) * b->sm_count));
-   g->rows_wide = rows_wide;
-   g->smem_wide = smem_for(rows_wide);
-   g->grid_wide = std::max(1, std::min(b->total, std::max(1, occupancy(rows_wide)) * b->sm_count));
-   g->wide = rows < rows_wide;
+   g->per_sm = occupancy(0, rows);
+   if (g->per_sm < 1) return bfail(b, PPI_ERR_UNSUPPORTED, "tile does not fit on an SM");
+   g->grid = std::max(1, std::min(b->total, g->per_sm * b->sm_count));
+   g->rows_wide = rows2;
+   g->smem_wide = smem_for(rows2);
+   g->grid_wide = std::max(1, std::min(b->total, std::max(1, occupancy(1, rows2)) * b->sm_count));
+   g->wide = rows < rows_max;
    return PPI_OK;
 }
 
@@ -233,42 +246,81 @@ ppi_status enqueue_step(ppi_batch* b, const int32_t* ph, const float* eph, const
    a.fitness = fit; a.pop_key = b->d_pop_key; a.pop_done = b->d_pop_done; a.best_index = best;
    a.stats = b->d_stats; a.n_main = b->d_n_main; a.status = b->d_status;
    a.rows = g.rows; a.wide_pass = 0;
-   PPI_BCUDA(b, launch_evaluate_batch(b->math, b->opset, a, g.block, g.grid, g.smem, s));
+   PPI_BCUDA(b, launch_evaluate_batch(b->math, b->opset, 0, a, g.block, g.grid, g.smem, s));
    if (g.wide) {
       a.rows = g.rows_wide; a.wide_pass = 1;
-      PPI_BCUDA(b, launch_evaluate_batch(b->math, b->opset, a, g.block, g.grid_wide, g.smem_wide, s));
+      PPI_BCUDA(b, launch_evaluate_batch(b->math, b->opset, 1, a, g.block, g.grid_wide, g.smem_wide, s));
    }
    return PPI_OK;
 }
 
-// Size the main pass's rows from a first evaluation's row histogram (all but
-// 1% of the work), then time both block shapes once on these inputs and keep
-// the faster.
+// Candidate main-pass row budgets for block size P: the most rows at each of
+// the three best occupancy levels (CTAs per SM).  More rows per CTA lowers
+// occupancy but keeps more programs out of the wide pass.
+std::vector<int> row_levels(ppi_batch* b, int P) {
+   std::vector<int> out;
+   BatchGeo g;
+   if (batch_geometry(b, P, 0, &g) != PPI_OK) return out;
+   int prev_occ = -1;
+   for (int rows = 1; rows <= g.fit + 1 && (int)out.size() < 3; ++rows) {
+      BatchGeo t;
+      const bool ok = rows <= g.fit && batch_geometry(b, P, rows, &t) == PPI_OK;
+      const int occ = ok ? t.per_sm : 0;
+      if (rows > 1 && occ != prev_occ) out.push_back(rows - 1);
+      if (!ok) break;
+      prev_occ = occ;
+   }
+   return out;
+}
+
+// Time the candidate shapes once on these inputs (twice when a step is
+// short) and keep the fastest: for 128-thread CTAs every occupancy level's
+// most rows, for 64-thread CTAs the level with the same shared memory per
+// warp as the best 128-thread shape.
 ppi_status autotune(ppi_batch* b, const int32_t* ph, const float* eph, const int32_t* size, float* fit,
                     int32_t* best, cudaStream_t s) {
-   ppi_status st = enqueue_step(b, ph, eph, size, fit, best, s, b->geo);
-   if (st != PPI_OK) return st;
-   PPI_BCUDA(b, cudaMemcpyAsync(b->h_rows, b->d_stats->rows_work, kRowBins * sizeof(unsigned long long),
-                                cudaMemcpyDeviceToHost, s));
-   PPI_BCUDA(b, cudaStreamSynchronize(s));
-   const int hint = rows_for_histogram(b->h_rows, kRowBins, 0.01);
-   int best_i = -1;
-   BatchGeo geos[2];
-   for (int i = 0; i < 2; ++i) {
-      if (batch_geometry(b, b->tune_blocks[i], hint, &geos[i]) != PPI_OK) {
-         b->tune_ms[i] = -1.0f;
-         continue;
-      }
-      PPI_BCUDA(b, cudaEventRecord(b->ev0, s));
-      st = enqueue_step(b, ph, eph, size, fit, best, s, geos[i]);
+   auto time_shape = [&](const BatchGeo& g, float* ms) -> ppi_status {
+      ppi_status st = enqueue_step(b, ph, eph, size, fit, best, s, g);   // warm
       if (st != PPI_OK) return st;
-      PPI_BCUDA(b, cudaEventRecord(b->ev1, s));
-      PPI_BCUDA(b, cudaEventSynchronize(b->ev1));
-      PPI_BCUDA(b, cudaEventElapsedTime(&b->tune_ms[i], b->ev0, b->ev1));
-      if (best_i < 0 || b->tune_ms[i] < b->tune_ms[best_i]) best_i = i;
+      float t = 0.0f;
+      for (int rep = 0; rep < 2; ++rep) {
+         PPI_BCUDA(b, cudaEventRecord(b->ev0, s));
+         st = enqueue_step(b, ph, eph, size, fit, best, s, g);
+         if (st != PPI_OK) return st;
+         PPI_BCUDA(b, cudaEventRecord(b->ev1, s));
+         PPI_BCUDA(b, cudaEventSynchronize(b->ev1));
+         float one = 0.0f;
+         PPI_BCUDA(b, cudaEventElapsedTime(&one, b->ev0, b->ev1));
+         t = rep == 0 ? one : std::min(t, one);
+         if (one > 50.0f) break;   // long steps: one timing is enough
+      }
+      *ms = t;
+      return PPI_OK;
+   };
+   BatchGeo best_g;
+   float best_ms = -1.0f;
+   b->tune_ms[0] = b->tune_ms[1] = -1.0f;
+   for (int r : row_levels(b, 128)) {
+      BatchGeo g;
+      if (batch_geometry(b, 128, r, &g) != PPI_OK) continue;
+      float ms;
+      ppi_status st = time_shape(g, &ms);
+      if (st != PPI_OK) return st;
+      if (b->tune_ms[1] < 0.0f || ms < b->tune_ms[1]) b->tune_ms[1] = ms;
+      if (best_ms < 0.0f || ms < best_ms) { best_ms = ms; best_g = g; }
    }
-   if (best_i < 0) return bfail(b, PPI_ERR_UNSUPPORTED, "no block shape fits this batch");
-   b->geo = geos[best_i];
+   // 64-thread CTAs: twice the rows of the best 128-thread shape fit in the
+   // same shared memory per warp
+   BatchGeo g64;
+   if (batch_geometry(b, 64, best_ms < 0.0f ? 0 : 2 * best_g.rows, &g64) == PPI_OK) {
+      float ms;
+      ppi_status st = time_shape(g64, &ms);
+      if (st != PPI_OK) return st;
+      b->tune_ms[0] = ms;
+      if (best_ms < 0.0f || ms < best_ms) { best_ms = ms; best_g = g64; }
+   }
+   if (best_ms < 0.0f) return bfail(b, PPI_ERR_UNSUPPORTED, "no block shape fits this batch");
+   b->geo = best_g;
    b->tuned = true;
    return PPI_OK;
 }
@@ -286,7 +338,7 @@ ppi_status ppi_batch_create(const ppi_gpu_config* c, int32_t n_pops, const ppi_b
    long long total = 0;
    for (int p = 0; p < n_pops; ++p) {
       const ppi_batch_population& q = pops[p];
-      if (!q.rows || q.nlin < 1 || q.ncol < 1 || q.n < 1 || q.strategy < 0 || q.strategy > 2 ||
+      if (!q.rows || q.nlin < 1 || q.ncol < 1 || q.ncol > kMaxColumns || q.n < 1 || q.strategy < 0 || q.strategy > 2 ||
           q.error_fn < 0 || q.error_fn > 3 || q.lanes > kMaxLanes ||
           (q.error_fn == PPI_EF_COST && (!q.cost || q.cost_n < 1 || q.cost_n > 4096)))
          return PPI_ERR_INVALID_ARGUMENT;
@@ -373,8 +425,7 @@ ppi_status ppi_batch_create(const ppi_gpu_config* c, int32_t n_pops, const ppi_b
        balloc(&b->d_meta, T) != cudaSuccess || balloc(&b->d_work, T * 2 * ms) != cudaSuccess ||
        cudaMallocHost(reinterpret_cast<void**>(&b->h_fit), T * 4) != cudaSuccess ||
        cudaMallocHost(reinterpret_cast<void**>(&b->h_best), (size_t)n_pops * 4) != cudaSuccess ||
-       cudaMallocHost(reinterpret_cast<void**>(&b->h_status), 4) != cudaSuccess ||
-       cudaMallocHost(reinterpret_cast<void**>(&b->h_rows), kRowBins * sizeof(unsigned long long)) != cudaSuccess)
+       cudaMallocHost(reinterpret_cast<void**>(&b->h_status), 4) != cudaSuccess)
       return bail(PPI_ERR_OUT_OF_MEMORY);
    if (cudaMemcpy(b->d_pops, b->host_pops.data(), n_pops * sizeof(PopDesc), cudaMemcpyHostToDevice) != cudaSuccess ||
        cudaMemcpy(b->d_pop_of, pop_of.data(), T * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess)
@@ -481,10 +532,26 @@ ppi_status ppi_batch_last_kernel_ms(ppi_batch* b, float* ms) {
    return PPI_OK;
 }
 
-ppi_status ppi_batch_shape(const ppi_batch* b, int32_t* block, int32_t* grid, float* tune_ms) {
+ppi_status ppi_batch_set_shape(ppi_batch* b, int32_t block, int32_t rows) {
+   if (!b || (block != 64 && block != 128) || rows < 0) return PPI_ERR_INVALID_ARGUMENT;
+   PPI_BCUDA(b, cudaSetDevice(b->device));
+   BatchGeo g;
+   ppi_status st = batch_geometry(b, block, rows, &g);
+   if (st != PPI_OK) return st;
+   b->geo = g;
+   b->tuned = true;   // a fixed shape is not re-tuned
+   return PPI_OK;
+}
+
+ppi_status ppi_batch_shape(const ppi_batch* b, int32_t* block, int32_t* grid, int32_t* rows,
+                           float* tune_ms) {
    if (!b || !block || !grid) return PPI_ERR_INVALID_ARGUMENT;
    *block = b->geo.block;
    *grid = b->geo.grid;
+   if (rows) {
+      rows[0] = b->geo.rows;
+      rows[1] = b->geo.wide ? b->geo.rows_wide : b->geo.rows;
+   }
    if (tune_ms) {
       tune_ms[0] = b->tune_ms[0];
       tune_ms[1] = b->tune_ms[1];

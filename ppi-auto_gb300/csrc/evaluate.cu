@@ -8,21 +8,27 @@
 
 namespace ppi {
 
-cudaError_t launch_evaluate_fast(int opset, const EvalArgs& a, int block, int grid, size_t smem, cudaStream_t s);
-cudaError_t launch_evaluate_parity(int opset, const EvalArgs& a, int block, int grid, size_t smem, cudaStream_t s);
-cudaError_t launch_evaluate_native(int opset, const EvalArgs& a, int block, int grid, size_t smem, cudaStream_t s);
+cudaError_t launch_evaluate_fast(int opset, int direct, const EvalArgs& a, int block, int grid, size_t smem,
+                              cudaStream_t s);
 cudaError_t launch_predict_fast(int opset, const PredictArgs& a, int block, int grid, size_t smem, cudaStream_t s);
+cudaError_t launch_evaluate_batch_fast(int opset, int direct, const BatchArgs& a, int block, int grid,
+                                    size_t smem, cudaStream_t s);
+cudaError_t evaluate_occupancy_fast(int opset, int direct, int block, size_t smem, int* per_sm);
+cudaError_t evaluate_batch_occupancy_fast(int opset, int direct, int block, size_t smem, int* per_sm);
+cudaError_t launch_evaluate_parity(int opset, int direct, const EvalArgs& a, int block, int grid, size_t smem,
+                              cudaStream_t s);
 cudaError_t launch_predict_parity(int opset, const PredictArgs& a, int block, int grid, size_t smem, cudaStream_t s);
+cudaError_t launch_evaluate_batch_parity(int opset, int direct, const BatchArgs& a, int block, int grid,
+                                    size_t smem, cudaStream_t s);
+cudaError_t evaluate_occupancy_parity(int opset, int direct, int block, size_t smem, int* per_sm);
+cudaError_t evaluate_batch_occupancy_parity(int opset, int direct, int block, size_t smem, int* per_sm);
+cudaError_t launch_evaluate_native(int opset, int direct, const EvalArgs& a, int block, int grid, size_t smem,
+                              cudaStream_t s);
 cudaError_t launch_predict_native(int opset, const PredictArgs& a, int block, int grid, size_t smem, cudaStream_t s);
-cudaError_t launch_evaluate_batch_fast(int opset, const BatchArgs& a, int block, int grid, size_t smem, cudaStream_t s);
-cudaError_t launch_evaluate_batch_parity(int opset, const BatchArgs& a, int block, int grid, size_t smem, cudaStream_t s);
-cudaError_t launch_evaluate_batch_native(int opset, const BatchArgs& a, int block, int grid, size_t smem, cudaStream_t s);
-cudaError_t evaluate_occupancy_fast(int opset, int block, size_t smem, int* per_sm);
-cudaError_t evaluate_occupancy_parity(int opset, int block, size_t smem, int* per_sm);
-cudaError_t evaluate_occupancy_native(int opset, int block, size_t smem, int* per_sm);
-cudaError_t evaluate_batch_occupancy_fast(int opset, int block, size_t smem, int* per_sm);
-cudaError_t evaluate_batch_occupancy_parity(int opset, int block, size_t smem, int* per_sm);
-cudaError_t evaluate_batch_occupancy_native(int opset, int block, size_t smem, int* per_sm);
+cudaError_t launch_evaluate_batch_native(int opset, int direct, const BatchArgs& a, int block, int grid,
+                                    size_t smem, cudaStream_t s);
+cudaError_t evaluate_occupancy_native(int opset, int direct, int block, size_t smem, int* per_sm);
+cudaError_t evaluate_batch_occupancy_native(int opset, int direct, int block, size_t smem, int* per_sm);
 
 size_t evaluate_smem_bytes(int code_stride, int rows, int block, int R, int lanes, bool aligned) {
    const size_t T = (size_t)block * R;
@@ -32,12 +38,12 @@ size_t evaluate_smem_bytes(int code_stride, int rows, int block, int R, int lane
    return code + tile + (size_t)lanes * 4 + (((size_t)lanes + 15) & ~(size_t)15);
 }
 
-cudaError_t launch_evaluate(int math, int opset, const EvalArgs& a, int block, int grid, size_t smem,
-                            cudaStream_t s) {
+cudaError_t launch_evaluate(int math, int opset, int direct, const EvalArgs& a, int block, int grid,
+                            size_t smem, cudaStream_t s) {
    switch (math) {
-   case kMathParity: return launch_evaluate_parity(opset, a, block, grid, smem, s);
-   case kMathNative: return launch_evaluate_native(opset, a, block, grid, smem, s);
-   default: return launch_evaluate_fast(opset, a, block, grid, smem, s);
+   case kMathParity: return launch_evaluate_parity(opset, direct, a, block, grid, smem, s);
+   case kMathNative: return launch_evaluate_native(opset, direct, a, block, grid, smem, s);
+   default: return launch_evaluate_fast(opset, direct, a, block, grid, smem, s);
    }
 }
 
@@ -50,28 +56,28 @@ cudaError_t launch_predict(int math, int opset, const PredictArgs& a, int block,
    }
 }
 
-cudaError_t launch_evaluate_batch(int math, int opset, const BatchArgs& a, int block, int grid,
+cudaError_t launch_evaluate_batch(int math, int opset, int direct, const BatchArgs& a, int block, int grid,
                                   size_t smem, cudaStream_t s) {
    switch (math) {
-   case kMathParity: return launch_evaluate_batch_parity(opset, a, block, grid, smem, s);
-   case kMathNative: return launch_evaluate_batch_native(opset, a, block, grid, smem, s);
-   default: return launch_evaluate_batch_fast(opset, a, block, grid, smem, s);
+   case kMathParity: return launch_evaluate_batch_parity(opset, direct, a, block, grid, smem, s);
+   case kMathNative: return launch_evaluate_batch_native(opset, direct, a, block, grid, smem, s);
+   default: return launch_evaluate_batch_fast(opset, direct, a, block, grid, smem, s);
    }
 }
 
-cudaError_t evaluate_occupancy(int math, int opset, int block, size_t smem, int* per_sm) {
+cudaError_t evaluate_occupancy(int math, int opset, int direct, int block, size_t smem, int* per_sm) {
    switch (math) {
-   case kMathParity: return evaluate_occupancy_parity(opset, block, smem, per_sm);
-   case kMathNative: return evaluate_occupancy_native(opset, block, smem, per_sm);
-   default: return evaluate_occupancy_fast(opset, block, smem, per_sm);
+   case kMathParity: return evaluate_occupancy_parity(opset, direct, block, smem, per_sm);
+   case kMathNative: return evaluate_occupancy_native(opset, direct, block, smem, per_sm);
+   default: return evaluate_occupancy_fast(opset, direct, block, smem, per_sm);
    }
 }
 
-cudaError_t evaluate_batch_occupancy(int math, int opset, int block, size_t smem, int* per_sm) {
+cudaError_t evaluate_batch_occupancy(int math, int opset, int direct, int block, size_t smem, int* per_sm) {
    switch (math) {
-   case kMathParity: return evaluate_batch_occupancy_parity(opset, block, smem, per_sm);
-   case kMathNative: return evaluate_batch_occupancy_native(opset, block, smem, per_sm);
-   default: return evaluate_batch_occupancy_fast(opset, block, smem, per_sm);
+   case kMathParity: return evaluate_batch_occupancy_parity(opset, direct, block, smem, per_sm);
+   case kMathNative: return evaluate_batch_occupancy_native(opset, direct, block, smem, per_sm);
+   default: return evaluate_batch_occupancy_fast(opset, direct, block, smem, per_sm);
    }
 }
 
@@ -101,7 +107,7 @@ int resolve_lanes(int strategy, int lanes, int nlin, int sm_count) {
 }
 
 const char* plan_geometry(int strategy, int lanes, int math, int opset, int nlin, int ncol,
-                          int code_stride, int n_max, int sm_count, Geometry* g, int rows_hint) {
+                          int code_stride, int n_max, int sm_count, Geometry* g) {
    const int L = lanes;
    if (L < 1 || L > kMaxLanes) return "lane count out of range";
    // records per thread: kR (8 measured faster than 16 on GB300: more
@@ -118,10 +124,8 @@ const char* plan_geometry(int strategy, int lanes, int math, int opset, int nlin
    if (strategy == PPI_STRATEGY_DP && L > P * R)
       return "DP lanes above 1024 records per group are not supported";
    const int rows_max = max_program_rows(ncol);
-   // wide budget: every program row count up to rows_max if it fits in
-   // kSmemCap, else as many rows as fit (programs needing more take the
-   // generic form); a narrower block when not even one column fits
    auto aligned_for = [&](int p) { return strategy == PPI_STRATEGY_PDP && L == p * R; };
+   // rows that fit in kSmemCap next to the code and lane buffers
    auto rows_fit = [&](int p) {
       const size_t fixed = evaluate_smem_bytes(code_stride, 0, p, R, L, aligned_for(p)) -
                            (size_t)p * R * 4;
@@ -132,21 +136,26 @@ const char* plan_geometry(int strategy, int lanes, int math, int opset, int nlin
           !(strategy == PPI_STRATEGY_DP && L > (P / 2) * R))
       P /= 2;
    const bool aligned = aligned_for(P);
-   const int rows_wide = std::min(rows_max, rows_fit(P));
-   if (rows_wide < 1) return "lane buffers do not fit in shared memory";
-   auto occupancy = [&](int rows) {
+   const int fit = std::min(rows_max, rows_fit(P));
+   if (fit < 1) return "lane buffers do not fit in shared memory";
+   auto occupancy = [&](int direct, int rows) {
       int per_sm = 0;
       const size_t smem = evaluate_smem_bytes(code_stride, rows, P, R, L, aligned);
-      if (evaluate_occupancy(math, opset, P, smem, &per_sm) != cudaSuccess) return 0;
+      if (evaluate_occupancy(math, opset, direct, P, smem, &per_sm) != cudaSuccess) return 0;
       return per_sm;
    };
-   // main budget: the most rows at the occupancy of a one-row tile, or the
-   // hint when it asks for more
-   const int top = occupancy(1);
-   if (top < 1) return "evaluator does not fit on an SM";
-   int rows = 1;
-   while (rows < rows_wide && occupancy(rows + 1) >= top) ++rows;
-   if (rows_hint > rows) rows = std::min(rows_hint, rows_wide);
+   // the most rows at the occupancy of a one-row tile
+   auto best_rows = [&](int direct) {
+      const int top = occupancy(direct, 1);
+      int rows = 1;
+      while (rows < fit && occupancy(direct, rows + 1) >= top) ++rows;
+      return rows;
+   };
+   // main pass: programs whose columns all fit, lean kernel
+   const int rows = best_rows(0);
+   // second pass: the rest, with the columns that do not fit read directly
+   // (room at least for the deepest slot need and the target)
+   const int rows2 = std::max(best_rows(1), std::min(fit, kSlots + 1));
    g->lanes = L;
    g->block = P;
    g->R = R;
@@ -154,30 +163,16 @@ const char* plan_geometry(int strategy, int lanes, int math, int opset, int nlin
    g->aligned = aligned;
    g->rows = rows;
    g->smem = evaluate_smem_bytes(code_stride, rows, P, R, L, aligned);
-   g->per_sm[0] = occupancy(rows);
+   g->per_sm[0] = occupancy(0, rows);
    if (g->per_sm[0] < 1) return "evaluator does not fit on an SM";
    g->grid = std::max(1, std::min(n_max, g->per_sm[0] * sm_count));
-   g->wide = rows < rows_wide;
-   g->rows_wide = rows_wide;
-   g->smem_wide = evaluate_smem_bytes(code_stride, rows_wide, P, R, L, aligned);
-   g->per_sm[1] = occupancy(rows_wide);
+   g->wide = rows < rows_max;
+   g->rows_wide = rows2;
+   g->smem_wide = evaluate_smem_bytes(code_stride, rows2, P, R, L, aligned);
+   g->per_sm[1] = occupancy(1, rows2);
    if (g->per_sm[1] < 1) return "evaluator does not fit on an SM";
    g->grid_wide = std::max(1, std::min(n_max, g->per_sm[1] * sm_count));
    return nullptr;
-}
-
-int rows_for_histogram(const unsigned long long* rows_work, int rows_cap, double spill) {
-   double total = 0.0;
-   for (int r = 0; r < kRowBins; ++r) total += (double)rows_work[r];
-   if (total <= 0.0) return 1;
-   double above = total;
-   int r = 0;
-   while (r < kRowBins - 1) {
-      above -= (double)rows_work[r];
-      if (above <= spill * total) break;
-      ++r;
-   }
-   return std::max(1, std::min(r, rows_cap));
 }
 
 }  // namespace ppi

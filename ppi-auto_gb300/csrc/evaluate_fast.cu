@@ -4,20 +4,22 @@
 
 namespace ppi {
 template struct ev::Launch<kMathFast>;
-cudaError_t launch_evaluate_fast(int opset, const EvalArgs& a, int block, int grid, size_t smem, cudaStream_t s) {
-   return ev::Launch<kMathFast>::evaluate(opset, a, block, grid, smem, s);
+cudaError_t launch_evaluate_fast(int opset, int direct, const EvalArgs& a, int block, int grid, size_t smem,
+                              cudaStream_t s) {
+   return ev::Launch<kMathFast>::evaluate(opset, direct, a, block, grid, smem, s);
 }
 cudaError_t launch_predict_fast(int opset, const PredictArgs& a, int block, int grid, size_t smem, cudaStream_t s) {
    return ev::Launch<kMathFast>::predict(opset, a, block, grid, smem, s);
 }
-cudaError_t launch_evaluate_batch_fast(int opset, const BatchArgs& a, int block, int grid, size_t smem, cudaStream_t s) {
-   return ev::Launch<kMathFast>::evaluate_batch(opset, a, block, grid, smem, s);
+cudaError_t launch_evaluate_batch_fast(int opset, int direct, const BatchArgs& a, int block, int grid,
+                                    size_t smem, cudaStream_t s) {
+   return ev::Launch<kMathFast>::evaluate_batch(opset, direct, a, block, grid, smem, s);
 }
-cudaError_t evaluate_occupancy_fast(int opset, int block, size_t smem, int* per_sm) {
-   return ev::Launch<kMathFast>::occupancy(opset, block, smem, per_sm);
+cudaError_t evaluate_occupancy_fast(int opset, int direct, int block, size_t smem, int* per_sm) {
+   return ev::Launch<kMathFast>::occupancy(opset, direct, block, smem, per_sm);
 }
-cudaError_t evaluate_batch_occupancy_fast(int opset, int block, size_t smem, int* per_sm) {
-   return ev::Launch<kMathFast>::occupancy_batch(opset, block, smem, per_sm);
+cudaError_t evaluate_batch_occupancy_fast(int opset, int direct, int block, size_t smem, int* per_sm) {
+   return ev::Launch<kMathFast>::occupancy_batch(opset, direct, block, smem, per_sm);
 }
 
 }  // namespace ppi

@@ -52,6 +52,40 @@ __device__ __forceinline__ void load_row(const float* p, int P, float (&x)[R]) {
       x[4 * i] = u.x; x[4 * i + 1] = u.y; x[4 * i + 2] = u.z; x[4 * i + 3] = u.w;
    }
 }
+// The current tile's view of the dataset, for operands read directly from
+// global memory: base = data + tile's first record, avail = records from
+// there to the end of a column's storage (ld - first record), vec = 16-byte
+// loads allowed (tile base a multiple of 4 records; ld is one).
+struct Direct {
+   const float* base;
+   int ld, avail, vec;
+};
+
+// x = the operand of an instruction: tile row `imm`, or with kDirectColumn the
+// record column read from global memory (positions at or past ld read 0, as a
+// staged row has them).  Kernels built with D = 0 run only programs whose
+// columns are all staged, and carry no code for direct reads.
+template <int D, int R>
+__device__ __forceinline__ void load_operand(uint32_t imm, const float* mine, int T, int P, int tid,
+                                             const Direct& g, float (&x)[R]) {
+   if (!D || !(imm & kDirectColumn)) {
+      load_row(mine + (size_t)imm * T, P, x);
+      return;
+   }
+   const float* col = g.base + (size_t)(imm & ~kDirectColumn) * g.ld;
+#pragma unroll
+   for (int i = 0; i < R / 4; ++i) {
+      const int pos = (i * P + tid) * 4;
+      if (g.vec && pos + 3 < g.avail) {
+         const float4 u = __ldg(reinterpret_cast<const float4*>(col + pos));
+         x[4 * i] = u.x; x[4 * i + 1] = u.y; x[4 * i + 2] = u.z; x[4 * i + 3] = u.w;
+      } else {
+#pragma unroll
+         for (int q = 0; q < 4; ++q) x[4 * i + q] = (pos + q < g.avail) ? __ldg(col + pos + q) : 0.0f;
+      }
+   }
+}
+
 template <int R>
 __device__ __forceinline__ void store_row(float* p, int P, const float (&x)[R]) {
 #pragma unroll
@@ -77,6 +111,20 @@ __device__ __forceinline__ void store_row(float* p, int P, const float (&x)[R]) 
    X(PPI_OP_COS) X(PPI_OP_SQRT) X(PPI_OP_LOG)
 #define PPI_ARITH_BINARY(X) X(PPI_OP_ADD) X(PPI_OP_SUB) X(PPI_OP_MULT) X(PPI_OP_DIV)
 
+// Unary opcodes whose fast-math routine is long enough that R inlined copies
+// per case crowd the instruction cache (the interpreter is bound by
+// instruction fetch): their case rotates the R values through one copy.
+// Measured on the polynomial workload: +44% in fast math.  The native
+// intrinsics and the double-precision parity routines stay unrolled (rolling
+// measured slightly slower there).
+template <int OP, int MATH>
+__device__ constexpr bool roll_unary() {
+   return MATH == kMathFast &&
+          (OP == PPI_OP_EXP || OP == PPI_OP_EXP10 || OP == PPI_OP_EXP2 || OP == PPI_OP_SIN ||
+           OP == PPI_OP_COS || OP == PPI_OP_LOGISTIC || OP == PPI_OP_GAMMA || OP == PPI_OP_GAUSS ||
+           OP == PPI_OP_LOG || OP == PPI_OP_LOG10 || OP == PPI_OP_LOG2 || OP == PPI_OP_TAN);
+}
+
 #define PPI_RUN_FAST_NAME run_fast_full
 #define PPI_UNARY_LIST PPI_FULL_UNARY
 #define PPI_BINARY_LIST PPI_FULL_BINARY
@@ -97,11 +145,11 @@ __device__ __forceinline__ void store_row(float* p, int P, const float (&x)[R]) 
 #undef PPI_BINARY_LIST
 #undef PPI_WITH_ITE
 
-template <int MATH, int R, int OPSET>
+template <int MATH, int R, int OPSET, int D>
 __device__ __forceinline__ void run_fast(const uint2* __restrict__ code, float* mine, int T, int P,
-                                         float (&acc)[R], int prot) {
-   if constexpr (OPSET == kOpsetArith) run_fast_arith<MATH, R>(code, mine, T, P, acc, prot);
-   else run_fast_full<MATH, R>(code, mine, T, P, acc, prot);
+                                         int tid, const Direct& g, float (&acc)[R], int prot) {
+   if constexpr (OPSET == kOpsetArith) run_fast_arith<MATH, R, D>(code, mine, T, P, tid, g, acc, prot);
+   else run_fast_full<MATH, R, D>(code, mine, T, P, tid, g, acc, prot);
 }
 
 // ---- generic stack interpreter ----------------------------------------------
@@ -173,13 +221,24 @@ __device__ __noinline__ void run_generic(const uint2* __restrict__ code, const f
    }
 }
 
-// Stage the records [base, base + T) of the program's columns (tile rows
-// s .. s+k-1, from the code header) and of the target column (row s+k).
+// Stage the records [base, base + T) of the program's staged columns (tile
+// rows s .. s+k-1, from the code header) and of the target column (row s+k),
+// and prefetch into L2 the same records of the columns it reads directly.
 __device__ __forceinline__ void stage_tile(const float* data, int ncol, int ld, const uint2* s_code,
                                            float* s_tile, int base, int T, int tid, int P) {
    const bool vec = (base & 3) == 0;
    const uint2 hdr = s_code[0];
-   const int k = (int)hdr.x, s = (int)hdr.y;
+   const int k = (int)hdr.x, s = (int)(hdr.y & 0xFFFFu), d = (int)(hdr.y >> 16);
+   const int lines = T / 32;   // 128-byte lines of one column's tile segment
+   for (int q = tid; q < d * lines; q += P) {
+      const int jj = k + q / lines, line = q - (q / lines) * lines;
+      const uint2 pair = s_code[1 + (jj >> 1)];
+      const int cidx = (int)((jj & 1) ? pair.y : pair.x);
+      if (base + line * 32 < ld) {
+         const float* p = data + (size_t)cidx * ld + base + line * 32;
+         asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+      }
+   }
    for (int j = 0; j <= k; ++j) {
       const uint2 pair = s_code[1 + (j >> 1)];
       const int cidx = (j == k) ? ncol - 1 : (int)((j & 1) ? pair.y : pair.x);
@@ -242,7 +301,7 @@ struct Job {
 // target; row 0 is reused for the tile's errors once the program has run),
 // then, unless the lane == tile-position path applies, lanes floats of lane
 // accumulators and lanes bytes of lane-finished flags.
-template <int MATH, int R, int OPSET>
+template <int MATH, int R, int OPSET, int D>
 __device__ float evaluate_program(const Job& j, uint2* s_code, float* s_tile, int* status, int tid,
                                   int P) {
    const int T = P * R;
@@ -276,8 +335,9 @@ __device__ float evaluate_program(const Job& j, uint2* s_code, float* s_tile, in
    for (int i = tid; i < j.meta.y; i += P) s_code[i] = j.code[i];
    if (!aligned)
       for (int l = tid; l < L; l += P) { s_acc[l] = 0.0f; s_done[l] = 0; }
-   const uint2* prog = s_code + code_header((int)j.code[0].x);
-   const int trow = (int)(j.code[0].x + j.code[0].y);
+   const uint2 hdr = j.code[0];
+   const uint2* prog = s_code + code_header((int)hdr.x + (int)(hdr.y >> 16));
+   const int trow = (int)hdr.x + (int)(hdr.y & 0xFFFFu);
    float lacc[R];
 #pragma unroll
    for (int r = 0; r < R; ++r) lacc[r] = 0.0f;
@@ -290,7 +350,8 @@ __device__ float evaluate_program(const Job& j, uint2* s_code, float* s_tile, in
       __syncthreads();
       float v[R];
       if (kind != kKindGeneric) {
-         run_fast<MATH, R, OPSET>(prog, s_tile + tid * 4, T, P, v, j.prot);
+         const Direct g{j.data + base, j.ld, j.ld - base, (base & 3) == 0};
+         run_fast<MATH, R, OPSET, D>(prog, s_tile + tid * 4, T, P, tid, g, v, j.prot);
       } else {
          float tmp[R];
          run_generic<MATH, R>(prog, j.data, j.ld, base, P, tid, tmp, j.prot);
@@ -382,7 +443,7 @@ __device__ float evaluate_program(const Job& j, uint2* s_code, float* s_tile, in
 
 // One population: a persistent grid pulls program indices from a device
 // counter; the last CTA to finish turns the packed arg-min into the index.
-template <int MATH, int R, int OPSET>
+template <int MATH, int R, int OPSET, int D>
 __global__ void __launch_bounds__(128, 4) eval_kernel(const EvalArgs a) {
    extern __shared__ __align__(16) unsigned char smem_raw[];
    __shared__ int s_prog;
@@ -409,7 +470,7 @@ __global__ void __launch_bounds__(128, 4) eval_kernel(const EvalArgs a) {
       }
       j.size = a.size[prog];
       j.code = a.code + (size_t)prog * a.code_stride;
-      const float fit = evaluate_program<MATH, R, OPSET>(j, s_code, s_tile, a.status, tid, P);
+      const float fit = evaluate_program<MATH, R, OPSET, D>(j, s_code, s_tile, a.status, tid, P);
       if (tid == 0) {
          a.fitness[prog] = fit;
          atomicMin(a.best_key, fitness_key(fit, prog));
@@ -430,7 +491,7 @@ __global__ void __launch_bounds__(128, 4) eval_kernel(const EvalArgs a) {
 // in cost order (size x records, largest first); each population keeps its
 // own arg-min key and completion counter, and the CTA that finishes a
 // population's last program writes that population's best index.
-template <int MATH, int R, int OPSET>
+template <int MATH, int R, int OPSET, int D>
 __global__ void __launch_bounds__(128, 4) eval_batch_kernel(const BatchArgs a) {
    extern __shared__ __align__(16) unsigned char smem_raw[];
    __shared__ int s_item;
@@ -456,7 +517,7 @@ __global__ void __launch_bounds__(128, 4) eval_batch_kernel(const BatchArgs a) {
       j.size = a.size[g];
       j.code = a.code + (size_t)g * a.code_stride;
       j.rows_cap = a.rows;
-      const float fit = evaluate_program<MATH, R, OPSET>(j, s_code, s_tile, a.status, tid, P);
+      const float fit = evaluate_program<MATH, R, OPSET, D>(j, s_code, s_tile, a.status, tid, P);
       if (tid == 0) {
          const int local = g - pd.prog_begin;
          a.fitness[g] = fit;
@@ -482,7 +543,8 @@ __global__ void __launch_bounds__(128, 4) predict_kernel(const PredictArgs a) {
    for (int i = tid; i < m.y; i += P) s_code[i] = a.code[i];
    const int kind = meta_kind(m);
    const bool runs = kind == kKindFast || kind == kKindWide || kind == kKindGeneric;
-   const uint2* prog = s_code + (runs ? code_header((int)a.code[0].x) : 0);
+   const uint2 hdr = runs ? a.code[0] : make_uint2(0u, 0u);
+   const uint2* prog = s_code + (runs ? code_header((int)hdr.x + (int)(hdr.y >> 16)) : 0);
    for (int base = blockIdx.x * T; base < a.nlin; base += gridDim.x * T) {
       __syncthreads();
       if (runs)
@@ -490,7 +552,8 @@ __global__ void __launch_bounds__(128, 4) predict_kernel(const PredictArgs a) {
       __syncthreads();
       float v[R];
       if (kind == kKindFast || kind == kKindWide) {
-         run_fast<MATH, R, OPSET>(prog, s_tile + tid * 4, T, P, v, a.prot);
+         const Direct g{a.data + base, a.ld, a.ld - base, (base & 3) == 0};
+         run_fast<MATH, R, OPSET, 1>(prog, s_tile + tid * 4, T, P, tid, g, v, a.prot);
       } else if (kind == kKindGeneric) {
          float tmp[R];
          run_generic<MATH, R>(prog, a.data, a.ld, base, P, tid, tmp, a.prot);
@@ -509,59 +572,68 @@ __global__ void __launch_bounds__(128, 4) predict_kernel(const PredictArgs a) {
 }
 
 
-template <int MATH, int OPSET>
-cudaError_t configure_t() {
-   cudaError_t e = cudaFuncSetAttribute(eval_kernel<MATH, kR, OPSET>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-   if (e != cudaSuccess) return e;
-   return cudaFuncSetAttribute(predict_kernel<MATH, kR, OPSET>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-}
-
 // Per-math entry points, instantiated in evaluate_<math>.cu (R = kR records
-// per thread; opset 0 = FULL, 1 = ARITH).
+// per thread; opset 0 = FULL, 1 = ARITH; direct 0 = every column staged,
+// 1 = direct column reads compiled in).
 template <int MATH>
 struct Launch {
+   using EvalFn = void (*)(const EvalArgs);
+   using BatchFn = void (*)(const BatchArgs);
+   using PredictFn = void (*)(const PredictArgs);
+   static EvalFn eval_fn(int opset, int direct) {
+      return opset ? (direct ? eval_kernel<MATH, kR, kOpsetArith, 1> : eval_kernel<MATH, kR, kOpsetArith, 0>)
+                   : (direct ? eval_kernel<MATH, kR, kOpsetFull, 1> : eval_kernel<MATH, kR, kOpsetFull, 0>);
+   }
+   static BatchFn batch_fn(int opset, int direct) {
+      return opset ? (direct ? eval_batch_kernel<MATH, kR, kOpsetArith, 1> : eval_batch_kernel<MATH, kR, kOpsetArith, 0>)
+                   : (direct ? eval_batch_kernel<MATH, kR, kOpsetFull, 1> : eval_batch_kernel<MATH, kR, kOpsetFull, 0>);
+   }
+   static PredictFn predict_fn(int opset) {
+      return opset ? predict_kernel<MATH, kR, kOpsetArith> : predict_kernel<MATH, kR, kOpsetFull>;
+   }
+   // Allow up to 200 KB of dynamic shared memory, once per kernel.
    static cudaError_t configure(int opset) {
       static bool done[2] = {false, false};
       if (done[opset]) return cudaSuccess;
-      cudaError_t e = opset ? configure_t<MATH, kOpsetArith>() : configure_t<MATH, kOpsetFull>();
-      if (e != cudaSuccess) return e;
-      e = cudaFuncSetAttribute(opset ? eval_batch_kernel<MATH, kR, kOpsetArith> : eval_batch_kernel<MATH, kR, kOpsetFull>,
-                               cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+      const int attr = cudaFuncAttributeMaxDynamicSharedMemorySize, bytes = 200 * 1024;
+      for (int direct = 0; direct < 2; ++direct) {
+         cudaError_t e = cudaFuncSetAttribute(eval_fn(opset, direct), (cudaFuncAttribute)attr, bytes);
+         if (e == cudaSuccess) e = cudaFuncSetAttribute(batch_fn(opset, direct), (cudaFuncAttribute)attr, bytes);
+         if (e != cudaSuccess) return e;
+      }
+      cudaError_t e = cudaFuncSetAttribute(predict_fn(opset), (cudaFuncAttribute)attr, bytes);
       if (e == cudaSuccess) done[opset] = true;
       return e;
    }
-   static cudaError_t evaluate(int opset, const EvalArgs& a, int block, int grid, size_t smem, cudaStream_t s) {
+   static cudaError_t evaluate(int opset, int direct, const EvalArgs& a, int block, int grid, size_t smem,
+                               cudaStream_t s) {
       cudaError_t e = configure(opset);
       if (e != cudaSuccess) return e;
-      if (opset) eval_kernel<MATH, kR, kOpsetArith><<<grid, block, smem, s>>>(a);
-      else eval_kernel<MATH, kR, kOpsetFull><<<grid, block, smem, s>>>(a);
+      eval_fn(opset, direct)<<<grid, block, smem, s>>>(a);
       return cudaGetLastError();
    }
-   static cudaError_t evaluate_batch(int opset, const BatchArgs& a, int block, int grid, size_t smem, cudaStream_t s) {
+   static cudaError_t evaluate_batch(int opset, int direct, const BatchArgs& a, int block, int grid,
+                                     size_t smem, cudaStream_t s) {
       cudaError_t e = configure(opset);
       if (e != cudaSuccess) return e;
-      if (opset) eval_batch_kernel<MATH, kR, kOpsetArith><<<grid, block, smem, s>>>(a);
-      else eval_batch_kernel<MATH, kR, kOpsetFull><<<grid, block, smem, s>>>(a);
+      batch_fn(opset, direct)<<<grid, block, smem, s>>>(a);
       return cudaGetLastError();
    }
    static cudaError_t predict(int opset, const PredictArgs& a, int block, int grid, size_t smem, cudaStream_t s) {
       cudaError_t e = configure(opset);
       if (e != cudaSuccess) return e;
-      if (opset) predict_kernel<MATH, kR, kOpsetArith><<<grid, block, smem, s>>>(a);
-      else predict_kernel<MATH, kR, kOpsetFull><<<grid, block, smem, s>>>(a);
+      predict_fn(opset)<<<grid, block, smem, s>>>(a);
       return cudaGetLastError();
    }
-   static cudaError_t occupancy(int opset, int block, size_t smem, int* per_sm) {
+   static cudaError_t occupancy(int opset, int direct, int block, size_t smem, int* per_sm) {
       cudaError_t e = configure(opset);
       if (e != cudaSuccess) return e;
-      if (opset) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, eval_kernel<MATH, kR, kOpsetArith>, block, smem);
-      return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, eval_kernel<MATH, kR, kOpsetFull>, block, smem);
+      return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, eval_fn(opset, direct), block, smem);
    }
-   static cudaError_t occupancy_batch(int opset, int block, size_t smem, int* per_sm) {
+   static cudaError_t occupancy_batch(int opset, int direct, int block, size_t smem, int* per_sm) {
       cudaError_t e = configure(opset);
       if (e != cudaSuccess) return e;
-      if (opset) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, eval_batch_kernel<MATH, kR, kOpsetArith>, block, smem);
-      return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, eval_batch_kernel<MATH, kR, kOpsetFull>, block, smem);
+      return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, batch_fn(opset, direct), block, smem);
    }
 };
 

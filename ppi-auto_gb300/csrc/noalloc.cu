@@ -84,7 +84,7 @@ extern "C" ppi_status ppi_gpu_evaluate_noalloc(const ppi_gpu_config* c, const fl
       return PPI_ERR_INVALID_ARGUMENT;
    if (c->max_size < 1 || c->max_size > 65535 || c->strategy < 0 || c->strategy > 2 ||
        c->error_fn < 0 || c->error_fn > 3 || c->math < 0 || c->math > 2 || c->lanes > kMaxLanes ||
-       c->n_symbols < 0 || (c->n_symbols > 0 && !c->symbols) || n < 1 || nlin < 1 || ncol < 1 ||
+       c->n_symbols < 0 || (c->n_symbols > 0 && !c->symbols) || n < 1 || nlin < 1 || ncol < 1 || ncol > kMaxColumns ||
        ld < nlin || (ld & 3) != 0 || (reinterpret_cast<uintptr_t>(d_data) & 15) != 0 ||
        c->device < 0 || c->device >= kMaxDevices)
       return PPI_ERR_INVALID_ARGUMENT;
@@ -175,10 +175,10 @@ extern "C" ppi_status ppi_gpu_evaluate_noalloc(const ppi_gpu_config* c, const fl
    if (cudaMemsetAsync(stats, 0, sizeof(DevStats), s) != cudaSuccess) return PPI_ERR_CUDA;
    if (launch_translate(c->math, t, s) != cudaSuccess) return PPI_ERR_CUDA;
    e.rows = g.rows; e.wide_pass = 0; e.final_pass = g.wide ? 0 : 1;
-   if (launch_evaluate(c->math, g.opset, e, g.block, g.grid, g.smem, s) != cudaSuccess) return PPI_ERR_CUDA;
+   if (launch_evaluate(c->math, g.opset, 0, e, g.block, g.grid, g.smem, s) != cudaSuccess) return PPI_ERR_CUDA;
    if (g.wide) {
       e.rows = g.rows_wide; e.wide_pass = 1; e.final_pass = 1;
-      if (launch_evaluate(c->math, g.opset, e, g.block, g.grid_wide, g.smem_wide, s) != cudaSuccess)
+      if (launch_evaluate(c->math, g.opset, 1, e, g.block, g.grid_wide, g.smem_wide, s) != cudaSuccess)
          return PPI_ERR_CUDA;
    }
    return PPI_OK;

@@ -54,8 +54,6 @@ struct ppi_gpu {
    float* h_fit = nullptr;
    int32_t* h_best = nullptr;
    int* h_status = nullptr;
-   unsigned long long* h_rows = nullptr;   // row histogram of the last evaluation
-   int rows_hint = 0;                      // main-pass row budget asked of plan_geometry
    // pending split call
    bool pending = false;
    int pending_n = 0;
@@ -100,7 +98,7 @@ void free_all(ppi_gpu* h) {
    cudaFree(h->d_stats); cudaFree(h->d_wide); cudaFree(h->d_best); cudaFree(h->d_status); cudaFree(h->d_pred);
    cudaFree(h->d_genomes); cudaFree(h->d_frames);
    free_decode_tables(&h->dec);
-   cudaFreeHost(h->h_fit); cudaFreeHost(h->h_best); cudaFreeHost(h->h_status); cudaFreeHost(h->h_rows);
+   cudaFreeHost(h->h_fit); cudaFreeHost(h->h_best); cudaFreeHost(h->h_status);
    if (h->ev0) cudaEventDestroy(h->ev0);
    if (h->ev1) cudaEventDestroy(h->ev1);
    if (h->evm) cudaEventDestroy(h->evm);
@@ -111,21 +109,10 @@ void free_all(ppi_gpu* h) {
 ppi_status plan(ppi_gpu* h) {
    Geometry g;
    const char* why = plan_geometry(h->cfg.strategy, h->lanes, h->cfg.math, h->opset, h->nlin,
-                                   h->ncol, h->code_stride, h->cfg.population_size, h->sm_count, &g,
-                                   h->rows_hint);
+                                   h->ncol, h->code_stride, h->cfg.population_size, h->sm_count, &g);
    if (why) return fail(h, PPI_ERR_UNSUPPORTED, why);
    h->geo = g;
    return PPI_OK;
-}
-
-// The next generation's programs resemble this one's: size the main pass's
-// rows to cover all but 1% of the work of the evaluation just read back
-// (h_rows).  Changes speed only, never a result.
-ppi_status update_rows_hint(ppi_gpu* h) {
-   const int hint = rows_for_histogram(h->h_rows, h->geo.rows_wide, 0.01);
-   if (hint == h->rows_hint) return PPI_OK;
-   h->rows_hint = hint;
-   return plan(h);
 }
 
 ppi_status check_ready(ppi_gpu* h, int n) {
@@ -161,11 +148,11 @@ ppi_status enqueue(ppi_gpu* h, const int32_t* d_ph, const float* d_eph, const in
    PPI_CUDA(h, launch_translate(h->cfg.math, t, s));
    PPI_CUDA(h, cudaEventRecord(h->evm, s));
    e.rows = g.rows; e.wide_pass = 0; e.final_pass = g.wide ? 0 : 1;
-   PPI_CUDA(h, launch_evaluate(h->cfg.math, g.opset, e, g.block, std::min(g.grid, n), g.smem, s));
+   PPI_CUDA(h, launch_evaluate(h->cfg.math, g.opset, 0, e, g.block, std::min(g.grid, n), g.smem, s));
    h->last_launches = 2;
    if (g.wide) {
       e.rows = g.rows_wide; e.wide_pass = 1; e.final_pass = 1;
-      PPI_CUDA(h, launch_evaluate(h->cfg.math, g.opset, e, g.block, std::min(g.grid_wide, n),
+      PPI_CUDA(h, launch_evaluate(h->cfg.math, g.opset, 1, e, g.block, std::min(g.grid_wide, n),
                                   g.smem_wide, s));
       h->last_launches = 3;
    }
@@ -233,7 +220,6 @@ ppi_status ppi_gpu_create(const ppi_gpu_config* c, ppi_gpu** out) {
        dalloc(&h->d_fit, pop) != cudaSuccess || dalloc(&h->d_key, 1) != cudaSuccess ||
        dalloc(&h->d_stats, 1) != cudaSuccess || dalloc(&h->d_wide, pop) != cudaSuccess ||
        dalloc(&h->d_best, 1) != cudaSuccess || dalloc(&h->d_status, 1) != cudaSuccess ||
-       cudaMallocHost(reinterpret_cast<void**>(&h->h_rows), kRowBins * sizeof(unsigned long long)) != cudaSuccess ||
        cudaMallocHost(reinterpret_cast<void**>(&h->h_fit), pop * sizeof(float)) != cudaSuccess ||
        cudaMallocHost(reinterpret_cast<void**>(&h->h_best), sizeof(int32_t)) != cudaSuccess ||
        cudaMallocHost(reinterpret_cast<void**>(&h->h_status), sizeof(int)) != cudaSuccess)
@@ -268,7 +254,8 @@ ppi_status ppi_gpu_set_dataset_rowmajor(ppi_gpu* h, const float* data, int32_t n
 
 ppi_status ppi_gpu_set_dataset(ppi_gpu* h, const float* const* rows, int32_t nlin, int32_t ncol) {
    if (!h) return PPI_ERR_INVALID_ARGUMENT;
-   if (!rows || nlin < 1 || ncol < 1) return fail(h, PPI_ERR_INVALID_ARGUMENT, "bad dataset");
+   if (!rows || nlin < 1 || ncol < 1 || ncol > kMaxColumns)
+      return fail(h, PPI_ERR_INVALID_ARGUMENT, "bad dataset");
    if (h->pending) return fail(h, PPI_ERR_NOT_READY, "an evaluate_launch is still pending");
    PPI_CUDA(h, cudaSetDevice(h->device));
    const int ld = (nlin + kColumnPad - 1) / kColumnPad * kColumnPad;
@@ -293,7 +280,6 @@ ppi_status ppi_gpu_set_dataset(ppi_gpu* h, const float* const* rows, int32_t nli
    const int L = resolve_lanes(h->cfg.strategy, h->cfg.lanes, nlin, h->sm_count);
    if (L < 1 || L > kMaxLanes) return fail(h, PPI_ERR_UNSUPPORTED, "lane count out of range");
    h->lanes = L;
-   h->rows_hint = 0;
    ppi_status s = plan(h);
    if (s != PPI_OK) return s;
    h->have_data = true;
@@ -316,8 +302,6 @@ ppi_status ppi_gpu_evaluate_launch(ppi_gpu* h, const int32_t* ph, const float* e
    PPI_CUDA(h, cudaMemcpyAsync(h->h_fit, h->d_fit, (size_t)n * 4, cudaMemcpyDeviceToHost, h->stream));
    PPI_CUDA(h, cudaMemcpyAsync(h->h_best, h->d_best, 4, cudaMemcpyDeviceToHost, h->stream));
    PPI_CUDA(h, cudaMemcpyAsync(h->h_status, h->d_status, 4, cudaMemcpyDeviceToHost, h->stream));
-   PPI_CUDA(h, cudaMemcpyAsync(h->h_rows, h->d_stats->rows_work, kRowBins * sizeof(unsigned long long),
-                               cudaMemcpyDeviceToHost, h->stream));
    h->pending = true;
    h->pending_n = n;
    h->out_fit = fitness;
@@ -333,8 +317,6 @@ ppi_status ppi_gpu_evaluate_wait(ppi_gpu* h) {
    std::memcpy(h->out_fit, h->h_fit, (size_t)h->pending_n * sizeof(float));
    if (h->out_best) *h->out_best = *h->h_best;
    cudaEventElapsedTime(&h->last_ms, h->ev0, h->ev1);
-   ppi_status s = update_rows_hint(h);
-   if (s != PPI_OK) return s;
    if (*h->h_status & kStatusUnsupportedProgram)
       return fail(h, PPI_ERR_UNSUPPORTED,
                   "a malformed program needs a deeper stack than the generic interpreter's");
@@ -521,8 +503,6 @@ ppi_status ppi_gpu_decode_evaluate(ppi_gpu* h, const uint8_t* genomes, int32_t n
    s = enqueue(h, h->d_ph, h->d_eph, h->d_size, n, alpha, h->d_fit, h->d_best, h->stream);
    if (s != PPI_OK) return s;
    h->last_launches += 1;
-   PPI_CUDA(h, cudaMemcpyAsync(h->h_rows, h->d_stats->rows_work, kRowBins * sizeof(unsigned long long),
-                               cudaMemcpyDeviceToHost, h->stream));
    PPI_CUDA(h, cudaMemcpyAsync(h->h_fit, h->d_fit, (size_t)n * 4, cudaMemcpyDeviceToHost, h->stream));
    PPI_CUDA(h, cudaMemcpyAsync(h->h_best, h->d_best, 4, cudaMemcpyDeviceToHost, h->stream));
    PPI_CUDA(h, cudaMemcpyAsync(h->h_status, h->d_status, 4, cudaMemcpyDeviceToHost, h->stream));
@@ -532,8 +512,6 @@ ppi_status ppi_gpu_decode_evaluate(ppi_gpu* h, const uint8_t* genomes, int32_t n
    std::memcpy(fitness, h->h_fit, (size_t)n * sizeof(float));
    if (best_index) *best_index = *h->h_best;
    cudaEventElapsedTime(&h->last_ms, h->ev0, h->ev1);
-   s = update_rows_hint(h);
-   if (s != PPI_OK) return s;
    if (*h->h_status & kStatusUnsupportedProgram)
       return fail(h, PPI_ERR_UNSUPPORTED, "a program needs a deeper stack than supported");
    return PPI_OK;

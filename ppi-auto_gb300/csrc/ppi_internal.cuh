@@ -18,8 +18,6 @@ constexpr int kR = 8;
 // most kSlots runs on the bytecode path.  Every binary tree of at most 255
 // nodes fits in 6 slots.
 constexpr int kSlots = 6;
-// Row-count histogram bins of the translator's statistics.
-constexpr int kRowBins = 64;
 // Largest lane count (PDP work-items per program, DP records per group).
 constexpr int kMaxLanes = 4096;
 // Stack depth of the generic (stack) interpreter used for malformed programs
@@ -34,19 +32,28 @@ enum : int { kOpsetFull = 0, kOpsetArith = 1 };
 // Program kinds written by the translator.  meta.x = kind | rows << 8, where
 // rows is the number of shared-memory rows the program's tile needs; meta.y is
 // the length of its code (header included).  kKindWide: bytecode path, but
-// more rows than the main pass's budget, so it runs in the wide pass.
+// its columns do not all fit the main pass's tile, so it runs in the wide
+// pass (which reads the columns its tile cannot hold from global memory).
 enum : int { kKindInvalid = 0, kKindFast = 1, kKindGeneric = 2, kKindUnsupported = 3, kKindWide = 4 };
 __host__ __device__ __forceinline__ int meta_kind(int2 m) { return m.x & 0xFF; }
 __host__ __device__ __forceinline__ int meta_rows(int2 m) { return m.x >> 8; }
 
-// Code of one program: entry 0 is the header {k, s}: the program reads k
-// distinct record columns and needs s slot rows.  Entries 1 .. (k+1)/2 list
-// the columns, two per entry (.x, .y), in the order of their tile rows.  The
-// instructions follow.  Tile rows: 0 .. s-1 slots, s .. s+k-1 the listed
+// Code of one program: entry 0 is the header {k, s | d << 16}: the program
+// stages k record columns in its tile, needs s slot rows, and reads d more
+// columns directly from global memory.  Entries 1 .. (k+d+1)/2 list the k
+// staged columns, then the d direct ones, two per entry (.x, .y).  The
+// instructions follow.  Tile rows: 0 .. s-1 slots, s .. s+k-1 the staged
 // columns, s+k the target column (the last column of the dataset).  The
-// generic form has k = s = 0 (its attribute reads go to global memory) and
+// generic form has k = s = d = 0 (its attribute reads go to global memory) and
 // its tokens follow the header.
-__host__ __device__ __forceinline__ int code_header(int k) { return 1 + (k + 1) / 2; }
+__host__ __device__ __forceinline__ int code_header(int ncols) { return 1 + (ncols + 1) / 2; }
+// Operand immediates of M_LD_ROW / M_BR_L / M_BR_R with this bit set name a
+// record column read from global memory (low bits: the column index) instead
+// of a tile row.
+constexpr uint32_t kDirectColumn = 0x80000000u;
+// Largest dataset width of the bytecode path (column indices share 24 bits
+// with a reference count in the translator).
+constexpr int kMaxColumns = (1 << 24) - 1;
 
 // Translator statistics, zeroed before every translation.
 struct DevStats {
@@ -54,7 +61,6 @@ struct DevStats {
    unsigned finished;        // CTAs finished in the final pass
    unsigned wide;            // programs of the wide pass (plain evaluation)
    unsigned wide_queue;      // work queue of the wide pass
-   unsigned long long rows_work[kRowBins];   // work (program size x records) by row count
 };
 
 // Status bits reported by the kernels.
@@ -357,8 +363,11 @@ struct PredictArgs {
 
 // Evaluator launch geometry: lanes, block size P, records per thread R, and
 // for the main and the wide pass the row budget, dynamic shared memory and a
-// one-wave persistent grid.  wide == false when no program can need more
-// rows than the main pass has (the wide pass is not launched).
+// one-wave persistent grid.  The main pass runs the programs whose columns
+// all fit its tile, on kernels without direct column reads; the wide pass
+// the rest, on kernels that read the columns their tile cannot hold from
+// global memory.  wide == false when every program fits the main tile (the
+// wide pass is not launched).
 struct Geometry {
    int lanes = 1, block = 128, R = 8, opset = kOpsetFull;
    int rows = 1, grid = 1;
@@ -373,29 +382,25 @@ struct Geometry {
 int opset_for(const ppi_symbol_entry* symbols, int n);
 int resolve_lanes(int strategy, int lanes, int nlin, int sm_count);
 // Returns nullptr on success, else why the configuration is unsupported.
-// rows_hint > 0 asks for that main-pass row budget (clamped to what fits);
-// 0 takes the largest budget at full occupancy.
 const char* plan_geometry(int strategy, int lanes, int math, int opset, int nlin, int ncol,
-                          int code_stride, int n_max, int sm_count, Geometry* g, int rows_hint = 0);
-// Main-pass row budget for the work histogram of a previous translation:
-// the smallest budget that covers all but `spill` of the work.
-int rows_for_histogram(const unsigned long long* rows_work, int rows_cap, double spill);
+                          int code_stride, int n_max, int sm_count, Geometry* g);
 // Largest program row count on a dataset of ncol columns.
 inline int max_program_rows(int ncol) { return kSlots + ncol + 1; }
 
 // Kernel launchers (evaluate.cu / translate.cu).
 cudaError_t launch_translate(int math, const TranslateArgs& a, cudaStream_t s);
-cudaError_t launch_evaluate(int math, int opset, const EvalArgs& a, int block, int grid, size_t smem,
-                            cudaStream_t s);
+cudaError_t launch_evaluate(int math, int opset, int direct, const EvalArgs& a, int block, int grid,
+                            size_t smem, cudaStream_t s);
 cudaError_t launch_predict(int math, int opset, const PredictArgs& a, int block, int grid, size_t smem,
                            cudaStream_t s);
-cudaError_t launch_evaluate_batch(int math, int opset, const BatchArgs& a, int block, int grid,
-                                  size_t smem, cudaStream_t s);
+cudaError_t launch_evaluate_batch(int math, int opset, int direct, const BatchArgs& a, int block,
+                                  int grid, size_t smem, cudaStream_t s);
 cudaError_t launch_batch_order(const unsigned* bucket_count, unsigned* cursor,
                                const unsigned char* bucket_of, int* order, int total,
                                unsigned* n_main, cudaStream_t s);
-cudaError_t evaluate_occupancy(int math, int opset, int block, size_t smem, int* blocks_per_sm);
-cudaError_t evaluate_batch_occupancy(int math, int opset, int block, size_t smem, int* blocks_per_sm);
+cudaError_t evaluate_occupancy(int math, int opset, int direct, int block, size_t smem, int* blocks_per_sm);
+cudaError_t evaluate_batch_occupancy(int math, int opset, int direct, int block, size_t smem,
+                                     int* blocks_per_sm);
 size_t evaluate_smem_bytes(int code_stride, int rows, int block, int R, int lanes, bool aligned);
 
 }  // namespace ppi

@@ -169,30 +169,68 @@ __device__ int2 translate_program(const TranslateArgs& ta, int i, int sz) {
    if (depth != 1) malformed = true;
 
    // ---- columns: distinct record columns read, in order of first use ------
+   // The tile stages them all when they fit the pass's row budget; else the
+   // most-read ones, and the rest are read from global memory by the
+   // instructions that use them.
    const int cap = ta.code_stride;
    const int slots = malformed ? 0 : node_need(w[0]);
    bool fast = !malformed && slots <= kSlots && node_sub(w[0]) == sz;
-   int ncols = 0, rows = 0;
+   int ncols = 0, nstaged = 0, rows = 0;
    if (fast) {
-      uint32_t* cols = frames + ta.max_size;   // upper half: the walk below uses at most sz frames
+      // cols[j] = column | min(references, 127) << 24 | staged << 31; each
+      // attribute leaf's immediate temporarily holds its column's j
+      uint32_t* cols = frames + ta.max_size;   // upper half: pass 2 uses at most sz frames
       for (int p = 0; p < sz;) {
          const uint2 wn = w[p];
          const int op = node_op(wn);
          if (op == PPI_OP_LITERAL) { p += node_sub(wn); continue; }   // a folded subtree is one literal
          if (op == PPI_OP_ATTRIBUTE) {
             int j = 0;
-            while (j < ncols && cols[j] != wn.y) ++j;
-            if (j == ncols) cols[ncols++] = wn.y;
-            w[p].y = (uint32_t)(slots + j);                // its tile row
+            while (j < ncols && (cols[j] & 0xFFFFFFu) != wn.y) ++j;
+            if (j == ncols) cols[ncols++] = wn.y | (1u << 24);
+            else if (((cols[j] >> 24) & 0x7Fu) < 127u) cols[j] += 1u << 24;
+            w[p].y = (uint32_t)j;
          }
          ++p;
       }
-      rows = slots + ncols + 1;
-      if (rows > ta.rows_wide || code_header(ncols) >= cap) fast = false;
+      // the main pass when every column fits its tile, else the wide pass
+      // with as many columns staged as its tile holds
+      const bool main_pass = slots + ncols + 1 <= ta.rows_main;
+      const int budget = main_pass ? ta.rows_main : ta.rows_wide;
+      if (slots + 1 > budget || code_header(ncols) >= cap) fast = false;
       if (fast) {
-         code[0] = make_uint2((uint32_t)ncols, (uint32_t)slots);
-         for (int j = 0; j < ncols; j += 2)
-            code[1 + j / 2] = make_uint2(cols[j], j + 1 < ncols ? cols[j + 1] : 0u);
+         nstaged = min(ncols, budget - slots - 1);
+         for (int q = 0; q < nstaged; ++q) {
+            int pick = -1;
+            uint32_t most = 0;
+            for (int j = 0; j < ncols; ++j) {
+               const uint32_t c = (cols[j] >> 24) & 0x7Fu;
+               if (!(cols[j] >> 31) && (pick < 0 || c > most)) { pick = j; most = c; }
+            }
+            cols[pick] |= 0x80000000u;
+         }
+         rows = slots + nstaged + 1;
+         // header: staged columns (tile rows slots..), then the direct ones,
+         // two per entry from code[1]
+         uint32_t* list = reinterpret_cast<uint32_t*>(code + 1);
+         int e = 0;
+         for (int j = 0; j < ncols; ++j)
+            if (cols[j] >> 31) list[e++] = cols[j] & 0xFFFFFFu;
+         for (int j = 0; j < ncols; ++j)
+            if (!(cols[j] >> 31)) list[e++] = cols[j] & 0xFFFFFFu;
+         if (ncols & 1) list[ncols] = 0u;
+         code[0] = make_uint2((uint32_t)nstaged, (uint32_t)slots | ((uint32_t)(ncols - nstaged) << 16));
+         // operand of each column: its tile row, or the column read directly
+         int row = slots;
+         for (int j = 0; j < ncols; ++j)
+            cols[j] = (cols[j] >> 31) ? (uint32_t)row++ : (kDirectColumn | (cols[j] & 0xFFFFFFu));
+         for (int p = 0; p < sz;) {
+            const uint2 wn = w[p];
+            const int op = node_op(wn);
+            if (op == PPI_OP_LITERAL) { p += node_sub(wn); continue; }
+            if (op == PPI_OP_ATTRIBUTE) w[p].y = cols[wn.y];
+            ++p;
+         }
       }
    }
 
@@ -290,7 +328,7 @@ __device__ int2 translate_program(const TranslateArgs& ta, int i, int sz) {
       if (ncode > cap) fast = false;
    }
    if (fast) {
-      const int kind = rows <= ta.rows_main ? kKindFast : kKindWide;
+      const int kind = nstaged == ncols && rows <= ta.rows_main ? kKindFast : kKindWide;
       return make_int2(kind | (rows << 8), ncode);
    }
    // ---- generic form: tokens in evaluation order ---------------------------
@@ -329,7 +367,6 @@ __global__ void translate_kernel(const TranslateArgs a) {
    a.meta[i] = m;
    const int kind = meta_kind(m);
    const unsigned long long work = valid ? (unsigned long long)sz * (unsigned long long)nlin : 0ull;
-   if (valid) atomicAdd(&a.stats->rows_work[min(meta_rows(m), kRowBins - 1)], work);
    if (a.pop_of) {
       // work order of a batch: cost buckets (cost = size x records), largest
       // first; the wide pass's programs in their own buckets

@@ -100,7 +100,7 @@ def test_batch_matches_plain_evaluations(gpu_lib, oracle_lib, math, flags):
                     ph[sl], ep[sl], sz[sl], p.get("strategy", "PDP"), lanes, alpha[k])
                 assert_bitexact(fit[sl], ref, "oracle, population %d" % k)
             begin += p["n"]
-    block, grid, tune = be.shape()
+    block, grid, rows, tune = be.shape()
     assert block in (64, 128) and grid >= 1
     if flags & ppi_gpu.BATCH_AUTOTUNE:
         assert max(tune) > 0.0

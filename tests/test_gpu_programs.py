@@ -203,13 +203,14 @@ def _sum_of_columns(gen, cols):
     return [(add, 0.0)] * (len(cols) - 1) + [(attr, float(c)) for c in cols]
 
 
-@pytest.mark.parametrize("strat,lanes", [("PDP", 0), ("PP", 0), ("DP", 64), ("PDP", 100)])
-def test_wide_dataset_main_wide_and_generic_tiles(gpu_lib, oracle_lib, strat, lanes):
-    """A 90-column dataset: programs reading a few columns fit the main pass's
-    tile, programs reading 20-40 distinct columns need the wide pass, and
-    ones reading 70+ columns exceed any tile and take the generic form.  The
-    second evaluation runs with the row budget re-planned from the first
-    one's histogram; both must match the oracle bit for bit."""
+@pytest.mark.parametrize("strat,lanes", [("PDP", 0), ("PP", 0), ("DP", 64), ("DP", 7), ("PDP", 100)])
+def test_wide_dataset_staged_and_direct_columns(gpu_lib, oracle_lib, strat, lanes):
+    """A 90-column dataset: programs reading a few columns stage them all in
+    the tile; programs reading 12-85 distinct columns stage the most-read
+    ones and read the rest directly from global memory (with DP over 7 lanes
+    the tiles start at records that are not multiples of 4, so those reads
+    are scalar).  The second evaluation runs with the row budget re-planned
+    from the first one's histogram; both must match the oracle bit for bit."""
     d = load_golden("allops")
     rng = np.random.default_rng(77 + lanes)
     rows = _dataset(rng, 3000, 90)
