@@ -1,31 +1,38 @@
 #!/usr/bin/env python3
-"""Benchmark of the population evaluator: GPop/s on one GB300.
+"""Benchmark of the population evaluator: GPop/s on one GB300, batched vs plain.
 
 Metric (the reference's own, src/interpreter/accelerator.cc:922): GPop/s =
 sum over programs of size[i] x records / evaluation time, i.e. opcode x record
 evaluations per second.
 
-Workload: the polynomial-regression configuration -- 100k records
-(x0 ~ U[-5,5], y = degree-4 polynomial with N(0,1) coefficients + N(0,0.01)
-noise), 30000 genomes of 8-bit codons decoded by the arithmetic+^2 grammar
-into programs of at most 128 opcodes, EF fabs((X)-(Y)), sum, protected
-functions, PDP strategy with the reference's lane rule (1024 work-items per
-program).  Synthetic data, seeded.
-
-A step is one evaluation of the whole population (what one acc_interpret
-call computes): translate + evaluate kernels, fitness + best index.
-  value : inputs resident in HBM, device time of K steps (CUDA events on the
-          launching stream), L2 flushed between steps outside the events;
-  e2e   : the same through ppi_gpu_evaluate with pinned host buffers: H2D of
-          phenotype/ephemeral/size and D2H of fitness + best index inside the
-          timed region (host wall clock, synchronous call).
-Multi-GPU (torchrun): every rank evaluates its own population (weak scaling,
-no collective on the data path); value = all ranks' GPop / max rank time.
+Default workload (--workload uneven): the uneven batch -- 64 independent
+populations of 256-30000 programs (log-uniform), program lengths 4-256
+opcodes (geometric, mean 40, random valid prefix trees over + - * / sin cos
+exp log sqrt ^2), datasets of 100-1M records x 1-32 N(0,1) features with
+targets from a random depth-5 expression + N(0,0.05) noise; EF
+fabs((X)-(Y)), sum, protected functions, PDP with the reference's lane rule.
+Synthetic data, seeded (no public dataset is involved).
+A step is one evaluation of every population:
+  value : the batched evaluator (ppi_batch_evaluate_device, one persistent
+          launch over all populations, CUDA graph, autotuned shape), inputs
+          resident in HBM, device time of K steps (CUDA events on the launching
+          stream), L2 flushed between steps outside the events;
+  plain : the same populations as 64 plain evaluations back to back
+          (ppi_gpu_evaluate_device per population), same timing; the line
+          asserts bit-identical fitness and best indices;
+  e2e   : the batched evaluator through ppi_batch_evaluate with pinned host
+          buffers: H2D of phenotype/ephemeral/size and D2H of fitness + best
+          indices inside the timed region (host wall clock, synchronous call).
+--workload polynomial: the polynomial-regression configuration (100k records,
+30000 genomes decoded on the GPU into programs <= 128 opcodes), one plain
+evaluation per step.
+Multi-GPU (torchrun): every rank evaluates its own batch (weak scaling, no
+collective on the data path); value = all ranks' GPop / max rank time.
 
 --impl reference times the reference's CPU implementation of the path (the
-oracle port of src/interpreter/sequential.cc + the OpenCL PP kernel's
-per-program loop, OpenMP over programs on all host cores) on a bounded sample
-of the same workload per step.
+oracle port of src/interpreter/sequential.cc + the OpenCL kernels' per-program
+loops, OpenMP over programs on all host cores) on a bounded sample of the same
+workload per step.
 """
 import argparse
 import json
@@ -103,15 +110,20 @@ def measured_peaks():
     return json.load(open(p)) if os.path.exists(p) else {}
 
 
-def profile_traffic(workload):
-    """Per-launch DRAM bytes of the evaluator kernel from a committed ncu summary."""
-    p = os.path.join(ROOT, "profiles", "eval_kernel_%s.md" % workload)
+def profile_value(name, key):
+    """A figure from a committed ncu summary (profiles/<name>.md, `key: value`)."""
+    p = os.path.join(ROOT, "profiles", name + ".md")
     if not os.path.exists(p):
         return None
     for line in open(p):
-        if line.startswith("traffic_bytes_per_launch:"):
+        if line.startswith(key + ":"):
             return float(line.split(":")[1])
     return None
+
+
+def profile_traffic(workload):
+    """Per-step DRAM bytes of the evaluator kernels from a committed ncu summary."""
+    return profile_value("eval_kernel_" + workload, "traffic_bytes_per_launch")
 
 
 def cpu_sample(wl, ph, eph, sz, budget_s, threads=0, chunk=200):
@@ -130,17 +142,83 @@ def cpu_sample(wl, ph, eph, sz, budget_s, threads=0, chunk=200):
         t += time.perf_counter() - t0
         ops += int(sz[done:done + k].sum()) * wl.nlin
         done += k
-    cores = threads if threads > 0 else (os.cpu_count() or 1)
     return ops / t / 1e9, done, cores, t
+
+
+def batch_cpu_sample(pops, sym, fraction, threads=0):
+    """Oracle port on the first programs of every population (a `fraction` of
+    each, and at least one per core: the port runs programs in parallel), all
+    records: (GPop/s, programs, cores, seconds)."""
+    from oracle import pyoracle
+    pyoracle.build()
+    cores = threads if threads > 0 else (os.cpu_count() or 1)
+    ops, t, done = 0, 0.0, 0
+    for p in pops:
+        k = min(p["n"], max(cores, int(round(p["n"] * fraction))))
+        o = pyoracle.Oracle(p["rows"], sym, p["error_fn"], None, False, p["protected"], False, threads)
+        lanes = min(p["rows"].shape[0], 1024)
+        t0 = time.perf_counter()
+        o.evaluate(p["phenotype"][:k], p["ephemeral"][:k], p["size"][:k], "PDP", lanes, 0.0)
+        t += time.perf_counter() - t0
+        ops += int(p["size"][:k].astype(np.int64).sum()) * p["rows"].shape[0]
+        done += k
+    return ops / t / 1e9, done, cores, t
+
+
+def batch_config(pops, work, extra):
+    nprog = sum(p["n"] for p in pops)
+    return dict({"workload": "uneven-batch-%dpops" % len(pops), "populations": len(pops),
+                 "programs": int(nprog),
+                 "records": [int(min(p["rows"].shape[0] for p in pops)),
+                             int(max(p["rows"].shape[0] for p in pops))],
+                 "features": [int(min(p["rows"].shape[1] - 1 for p in pops)),
+                              int(max(p["rows"].shape[1] - 1 for p in pops))],
+                 "max_size": 256, "mean_size": round(float(np.mean(np.concatenate(
+                     [p["size"] for p in pops]))), 2),
+                 "strategy": "PDP", "error_fn": "abs", "reduce_max": False, "protected": True,
+                 "ops_per_step": int(work)}, **extra)
 
 
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
         return 0
-    from ppi_gpu import workloads
     from oracle import pyoracle
     pyoracle.build()
+    if args.workload == "polynomial":
+        return run_reference_polynomial(args)
+    from ppi_gpu import workloads
+    g, pops = workloads.uneven_batch(seed=11, n_pops=args.populations,
+                                     pop_range=(256, args.max_programs))
+    sym = g.symbol_table_arrays()
+    work = float(sum(int(p["size"].sum()) * p["rows"].shape[0] for p in pops))
+    # each step: a bounded sample (the first programs of every population, all records)
+    frac = 0.002
+    vals = []
+    for k in range(args.warmup + args.steps):
+        v, n, cores, t = batch_cpu_sample(pops, sym, frac)
+        if k >= args.warmup:
+            vals.append((v, t))
+    value = float(np.mean([v for v, _ in vals]))
+    ms = float(np.mean([t for _, t in vals]) * 1e3)
+    sample = ("the first %.1f%% (at least one per core) of every population's programs (%d "
+              "programs) x all records per step" % (100 * frac, n))
+    line = {"impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": UNIT,
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(ms, 3), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+            "config": batch_config(pops, work, {"impl": "oracle port of the reference CPU interpreter"}),
+            "cpu_baseline": {"value": round(value, 4), "unit": UNIT, "cores": cores,
+                             "kind": "port", "sample": sample},
+            "e2e": {"value": round(value, 4), "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def run_reference_polynomial(args):
+    from ppi_gpu import workloads
+    from oracle import pyoracle
     wl = workloads.polynomial()
     ph, eph, sz = pyoracle.decode(wl.grammar, wl.genomes, wl.bits_per_gene,
                                   wl.bits_per_constant, wl.lo, wl.hi, wl.max_size)
@@ -158,7 +236,7 @@ def run_reference(args):
     sample = "%d programs of the %d-program population x all %d records per step" % (
         per_step, wl.population, wl.nlin)
     line = {"impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": UNIT,
-            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": round(ms, 3), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
             "config": dict(wl.describe(), impl="oracle port of the reference CPU interpreter"),
@@ -170,7 +248,185 @@ def run_reference(args):
     return 0
 
 
-def run_ours(args):
+def run_batch(args):
+    """The uneven batch: batched evaluator vs 64 plain evaluations."""
+    import torch
+    import ppi_gpu
+    from ppi_gpu import workloads
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    g, pops = workloads.uneven_batch(seed=11 + rank, n_pops=args.populations,
+                                     pop_range=(256, args.max_programs))
+    sym = g.symbol_table_arrays()
+    ph = np.concatenate([p["phenotype"] for p in pops])
+    eph = np.concatenate([p["ephemeral"] for p in pops])
+    sz = np.concatenate([p["size"] for p in pops])
+    work = float(sum(int(p["size"].sum()) * p["rows"].shape[0] for p in pops))
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.current_stream(dev)
+    sh = stream.cuda_stream
+    d_ph, d_eph, d_sz = [torch.from_numpy(a).to(dev) for a in (ph, eph, sz)]
+    n = len(sz)
+    d_fit = torch.empty(n, dtype=torch.float32, device=dev)
+    d_best = torch.empty(len(pops), dtype=torch.int32, device=dev)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)   # 256 MiB > L2
+    be = ppi_gpu.BatchEvaluator(sym, 256, pops, args.math, device=local)
+    flags = ppi_gpu.BATCH_GRAPH | ppi_gpu.BATCH_AUTOTUNE
+
+    def step():
+        be.evaluate_device(d_ph.data_ptr(), d_eph.data_ptr(), d_sz.data_ptr(), d_fit.data_ptr(),
+                           d_best.data_ptr(), sh, flags)
+
+    t0 = time.perf_counter()
+    for _ in range(args.warmup):          # the first step autotunes the shape
+        flush.zero_()
+        step()
+    torch.cuda.synchronize(dev)
+    warm_s = time.perf_counter() - t0
+
+    def timed(fn):
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+               for _ in range(args.steps)]
+        launches = 0
+        for k in range(args.steps):
+            flush.zero_()
+            evs[k][0].record(stream)
+            launches += fn()
+            evs[k][1].record(stream)
+        torch.cuda.synchronize(dev)
+        return [a.elapsed_time(b) for a, b in evs], launches
+
+    def batch_step():
+        step()
+        return be.last_launch_count()
+
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize(dev)
+    clocks = ClockSampler(local)
+    clocks.start()
+    step_ms, launches = timed(batch_step)
+    clk = clocks.stop()
+    if world > 1:
+        torch.distributed.barrier()
+    fit_b = d_fit.cpu().numpy().copy()
+    best_b = d_best.cpu().numpy().copy()
+
+    # plain: one evaluator per population, launched back to back
+    plain_evs, offs, begin = [], [], 0
+    for p in pops:
+        e = ppi_gpu.Evaluator(sym, 256, p["n"], "PDP", 0, "abs", None, False, True, args.math,
+                              device=local)
+        e.set_dataset(p["rows"])
+        plain_evs.append(e)
+        offs.append(begin)
+        begin += p["n"]
+    p_fit = torch.empty_like(d_fit)
+    p_best = torch.empty_like(d_best)
+
+    def plain_step():
+        cnt = 0
+        for k, (e, o, p) in enumerate(zip(plain_evs, offs, pops)):
+            e.evaluate_device(d_ph[o:].data_ptr(), d_eph[o:].data_ptr(), d_sz[o:].data_ptr(),
+                              p["n"], 0.0, p_fit[o:].data_ptr(), p_best[k:].data_ptr(), sh)
+            cnt += e.last_launch_count()
+        return cnt
+
+    for _ in range(args.warmup):
+        plain_step()
+    plain_ms, plain_launches = timed(plain_step)
+    equal = (np.array_equal(p_fit.cpu().numpy().view(np.int32), fit_b.view(np.int32)) and
+             np.array_equal(p_best.cpu().numpy(), best_b))
+    assert equal, "batched and plain fitness differ"
+    for e in plain_evs:
+        e.close()
+
+    # end to end through the C ABI with pinned host buffers
+    h_ph = torch.from_numpy(ph).pin_memory().numpy()
+    h_eph = torch.from_numpy(eph).pin_memory().numpy()
+    h_sz = torch.from_numpy(sz).pin_memory().numpy()
+    for _ in range(args.warmup):
+        be.evaluate(h_ph, h_eph, h_sz, flags)
+    if world > 1:
+        torch.distributed.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        fit_e, best_e = be.evaluate(h_ph, h_eph, h_sz, flags)
+    e2e_s = time.perf_counter() - t0
+    assert np.array_equal(fit_e.view(np.int32), fit_b.view(np.int32))
+
+    total_s = sum(step_ms) / 1e3
+    plain_s = sum(plain_ms) / 1e3
+    tot = torch.tensor([total_s, e2e_s, plain_s, work], dtype=torch.float64, device=dev)
+    if world > 1:
+        mx = tot.clone()
+        torch.distributed.all_reduce(mx[:3], op=torch.distributed.ReduceOp.MAX)
+        sm = tot.clone()
+        torch.distributed.all_reduce(sm[3:], op=torch.distributed.ReduceOp.SUM)
+        total_s, e2e_s, plain_s, all_ops = float(mx[0]), float(mx[1]), float(mx[2]), float(sm[3])
+    else:
+        all_ops = work
+    if rank != 0:
+        return 0
+    value = all_ops * args.steps / total_s / 1e9
+    plain_v = all_ops * args.steps / plain_s / 1e9
+    e2e = all_ops * args.steps / e2e_s / 1e9
+    peaks = measured_peaks()
+    sm_count = torch.cuda.get_device_properties(dev).multi_processor_count
+    max_mhz = float(peaks.get("sm_max_mhz", 2070.0))
+    peak = sm_count * 128 * max_mhz * 1e6 / 1e9          # FP32 lane-ops/s, in G
+    block, grid, rows, tune = be.shape()
+    kernel_ms = float(np.mean(step_ms))
+    cpu_v, cpu_n, cpu_cores, cpu_t = batch_cpu_sample(pops, sym, args.cpu_fraction)
+    issue = profile_value("eval_batch_kernel_uneven-batch-small", "issue_active_frac")
+    line = {
+        "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(total_s * 1e3 / args.steps, 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+        "config": batch_config(pops, work, {
+            "math": args.math, "block": block, "grid": grid, "tile_rows": list(rows),
+            "autotune_ms": [round(t, 2) for t in tune], "warmup_s": round(warm_s, 2),
+            "l2": "256 MiB buffer written between steps, outside the timed events; "
+                  "the batch's datasets (%.0f MB) exceed L2" % (
+                      sum(p["rows"].nbytes for p in pops) / 1e6)}),
+        "plain": {"value": round(plain_v, 3), "unit": UNIT,
+                  "ms_per_step": round(plain_s * 1e3 / args.steps, 4),
+                  "launches_per_step": plain_launches // args.steps,
+                  "speedup_batched_vs_plain": round(value / plain_v, 3),
+                  "equal_fitness": bool(equal)},
+        "e2e": {"value": round(e2e, 3), "unit": UNIT,
+                "h2d_bytes_per_step": int(ph.nbytes + eph.nbytes + sz.nbytes),
+                "d2h_bytes_per_step": int(n * 4 + len(pops) * 4 + 4)},
+        "gpu_launches": launches,
+        "roofline": {"bound": "fp32_issue", "achieved": round(all_ops / world / (kernel_ms / 1e3) / 1e9, 2),
+                     "peak": round(peak, 1), "unit": "Gop/s",
+                     "frac": round(all_ops / world / (kernel_ms / 1e3) / 1e9 / peak, 4),
+                     "peak_source": "SMs x 128 FP32 lanes x sm_max_mhz (MEASURED_PEAKS.json)",
+                     "kernel": "translate + work order + eval_batch_kernel main and wide pass "
+                               "(one graph launch per step)",
+                     "kernel_ms": round(kernel_ms, 4),
+                     "frac_at_median_clock": round(all_ops / world / (kernel_ms / 1e3) / 1e9 /
+                                                   (sm_count * 128 * clk["sm_mhz"] / 1e3), 4)
+                     if clk.get("sm_mhz") else None,
+                     "issue_active_frac": issue,
+                     "traffic": profile_traffic("uneven-batch")},
+        "cpu_baseline": {"value": round(cpu_v, 4), "unit": UNIT, "cores": cpu_cores,
+                         "kind": "port",
+                         "sample": "first %.1f%% (at least one per core) of every population's "
+                                   "programs (%d) x all records (%.1f s), oracle port, OpenMP "
+                                   "over programs" % (
+                                       100 * args.cpu_fraction, cpu_n, cpu_t)},
+        "clocks": clk,
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def run_polynomial(args):
     import torch
     import ppi_gpu
     from ppi_gpu import workloads
@@ -306,19 +562,26 @@ def run_ours(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--math", default="fast", choices=["fast", "parity", "native"])
+    ap.add_argument("--workload", default="uneven", choices=["uneven", "polynomial"])
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
-    # smaller cases of the same workload, for profiling captures only
+    ap.add_argument("--cpu-fraction", type=float, default=0.015,
+                    help="uneven batch: share of every population timed on the CPU")
+    # smaller cases of the same workloads, for profiling captures only
+    ap.add_argument("--populations", type=int, default=64)
+    ap.add_argument("--max-programs", type=int, default=30_000)
     ap.add_argument("--records", type=int, default=100_000)
     ap.add_argument("--population", type=int, default=30_000)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
     if args.impl == "reference":
         return run_reference(args)
-    return run_ours(args)
+    if args.workload == "polynomial":
+        return run_polynomial(args)
+    return run_batch(args)
 
 
 if __name__ == "__main__":

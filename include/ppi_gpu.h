@@ -244,6 +244,8 @@ ppi_status ppi_batch_evaluate_device(ppi_batch* b, const int32_t* d_phenotype,
                                      int32_t flags);
 /* Device time of the last step (waits for it). */
 ppi_status ppi_batch_last_kernel_ms(ppi_batch* b, float* ms);
+/* Kernels the last step launched (translator, work order, evaluator passes). */
+ppi_status ppi_batch_last_launch_count(const ppi_batch* b, int32_t* n);
 /* Block size and main-pass grid in use; rows (may be NULL) receives the tile
  * rows of the main and the wide pass; tune_ms (may be NULL) the autotuner's
  * timings of the 64- and 128-thread shapes at their best rows (-1: shape does

@@ -342,7 +342,7 @@ int ppio_evaluate(const ppio_config* c, int strategy, int lanes, const int32_t* 
          failed = 1;
       } else {
 #ifdef _OPENMP
-#pragma omp for schedule(dynamic, 4)
+#pragma omp for schedule(dynamic, 1)
 #endif
          for (int i = 0; i < n; ++i) {
             int sz = size[i];

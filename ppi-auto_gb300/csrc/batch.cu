@@ -130,6 +130,7 @@ struct ppi_batch {
    const void* graph_key[6] = {};
    cudaStream_t graph_stream = nullptr;
    float last_ms = 0.0f;
+   int last_launches = 0;   // kernels of the last step
 };
 
 namespace {
@@ -247,9 +248,11 @@ ppi_status enqueue_step(ppi_batch* b, const int32_t* ph, const float* eph, const
    a.stats = b->d_stats; a.n_main = b->d_n_main; a.status = b->d_status;
    a.rows = g.rows; a.wide_pass = 0;
    PPI_BCUDA(b, launch_evaluate_batch(b->math, b->opset, 0, a, g.block, g.grid, g.smem, s));
+   b->last_launches = 4;   // translate, order scan, order scatter, main pass
    if (g.wide) {
       a.rows = g.rows_wide; a.wide_pass = 1;
       PPI_BCUDA(b, launch_evaluate_batch(b->math, b->opset, 1, a, g.block, g.grid_wide, g.smem_wide, s));
+      b->last_launches = 5;
    }
    return PPI_OK;
 }
@@ -529,6 +532,12 @@ ppi_status ppi_batch_last_kernel_ms(ppi_batch* b, float* ms) {
    if (!b || !ms) return PPI_ERR_INVALID_ARGUMENT;
    PPI_BCUDA(b, cudaEventSynchronize(b->ev1));
    PPI_BCUDA(b, cudaEventElapsedTime(ms, b->ev0, b->ev1));
+   return PPI_OK;
+}
+
+ppi_status ppi_batch_last_launch_count(const ppi_batch* b, int32_t* n) {
+   if (!b || !n) return PPI_ERR_INVALID_ARGUMENT;
+   *n = b->last_launches;
    return PPI_OK;
 }
 

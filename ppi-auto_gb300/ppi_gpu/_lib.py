@@ -110,6 +110,7 @@ def load_library():
     L.ppi_batch_last_kernel_ms.argtypes = [C.c_void_p, _fp]
     L.ppi_batch_shape.argtypes = [C.c_void_p, _ip, _ip, _ip, _fp]
     L.ppi_batch_set_shape.argtypes = [C.c_void_p, C.c_int32, C.c_int32]
+    L.ppi_batch_last_launch_count.argtypes = [C.c_void_p, _ip]
     _lib = L
     return L
 
@@ -339,6 +340,11 @@ class BatchEvaluator:
         t = np.zeros(2, np.float32)
         self._check(self._L.ppi_batch_shape(self._h, _i(b), _i(g), _i(r), _f(t)))
         return int(b[0]), int(g[0]), (int(r[0]), int(r[1])), (float(t[0]), float(t[1]))
+
+    def last_launch_count(self):
+        n = np.zeros(1, np.int32)
+        self._check(self._L.ppi_batch_last_launch_count(self._h, _i(n)))
+        return int(n[0])
 
     def set_shape(self, block, rows=0):
         self._check(self._L.ppi_batch_set_shape(self._h, block, rows))
