@@ -202,6 +202,21 @@ int32_t ppi_gpu_lanes(const ppi_gpu* h);
 /* Number of kernel launches the last evaluate / predict / decode call made. */
 int32_t ppi_gpu_last_launch_count(const ppi_gpu* h);
 
+/* ---- constant adjoint --------------------------------------------------------
+ * No counterpart in the reference: an addition for refining the ephemeral
+ * constants of programs by gradient steps, while ppi_gpu_evaluate stays the
+ * fitness judge.  gradient (n x max_size) receives d(fitness)/d(ephemeral[i][k])
+ * at every CONST token k of program i and 0 at the other tokens, for the
+ * fitness (1/nlin) sum_n EF(X_n, Y_n) of the handle's dataset: the sum
+ * reduction (REDUCEMAX is rejected) with the absolute or squared error (other
+ * error functions are piecewise constant in X and are rejected).  The forward
+ * sweep runs in the handle's math mode.  A program whose error is non-finite
+ * on some record (its fitness is the FLT_MAX sentinel) gets a zero gradient;
+ * a malformed program, or one with more than 32 constants, gets NaN.
+ * Synchronous. */
+ppi_status ppi_gpu_constant_gradient(ppi_gpu* h, const int32_t* phenotype, const float* ephemeral,
+                                     const int32_t* size, int32_t n, float* gradient);
+
 /* ---- batches: many populations in one launch ------------------------------
  * No single reference function: this evaluates what several acc_interpret
  * calls would (one per population, e.g. one per island or per independent

@@ -457,3 +457,259 @@ int ppio_decode(const int32_t* rule_first, const int32_t* rule_count, const int3
    }
    return 0;
 }
+
+/* One operator in the reference's float semantics (the switch of
+ * eval_record, with the operands as separate values: a = stack[top],
+ * b = stack[top-1], c = stack[top-2]). */
+static float f_node(int op, float a, float b, float c, int prot, int fm) {
+   switch (op) {
+   case OP_IF_THEN_ELSE: return truthy(a) ? b : c;
+   case OP_AND: return (truthy(a) && truthy(b)) ? 1.0f : 0.0f;
+   case OP_OR: return (truthy(a) || truthy(b)) ? 1.0f : 0.0f;
+   case OP_XOR: return (!truthy(a) != !truthy(b)) ? 1.0f : 0.0f;
+   case OP_GREATER: return (a > b) ? 1.0f : 0.0f;
+   case OP_GREATEREQUAL: return (a >= b) ? 1.0f : 0.0f;
+   case OP_LESS: return (a < b) ? 1.0f : 0.0f;
+   case OP_LESSEQUAL: return (a <= b) ? 1.0f : 0.0f;
+   case OP_EQUAL: return (a == b) ? 1.0f : 0.0f;
+   case OP_NOTEQUAL: return (a != b) ? 1.0f : 0.0f;
+   case OP_ADD: return a + b;
+   case OP_SUB: return a - b;
+   case OP_MULT: return a * b;
+   case OP_MEAN: return (a + b) / 2.0f;
+   case OP_MAX: return fmaxf(a, b);
+   case OP_MIN: return fminf(a, b);
+   case OP_MOD: return fmodf(a, b);
+   case OP_POW: return f_pow(a, b, fm);
+   case OP_DIV: return f_div(a, b, prot);
+   case OP_NOT: return truthy(a) ? 0.0f : 1.0f;
+   case OP_ABS: return fabsf(a);
+   case OP_POW2: return a * a;
+   case OP_POW3: return a * a * a;
+   case OP_POW4: return a * a * a * a;
+   case OP_POW5: return a * a * a * a * a;
+   case OP_NEG: return -a;
+   case OP_ROUND: return roundf(a);
+   case OP_CEIL: return ceilf(a);
+   case OP_FLOOR: return floorf(a);
+   case OP_EXP: return m_exp(a, fm);
+   case OP_EXP10: return m_exp10(a, fm);
+   case OP_EXP2: return m_exp2(a, fm);
+   case OP_SIN: return m_sin(a, fm);
+   case OP_COS: return m_cos(a, fm);
+   case OP_STEP: return (a >= 0.0f) ? 1.0f : 0.0f;
+   case OP_SIGN: return a > 0.0f ? 1.0f : (a < 0.0f ? -1.0f : 0.0f);
+   case OP_LOGISTIC: return 1.0f / (1.0f + m_exp(-a, fm));
+   case OP_GAMMA: return f_gamma(a, prot, fm);
+   case OP_GAUSS: return m_exp(-a * a, fm);
+   case OP_SQRT: return f_sqrt(a, prot, fm);
+   case OP_LOG: return f_log(a, prot, fm);
+   case OP_LOG10: return f_log10(a, prot, fm);
+   case OP_LOG2: return f_log2(a, prot, fm);
+   case OP_TAN: return f_tan(a, prot, fm);
+   default: return NAN;
+   }
+}
+
+/* ---- FP64 constant adjoint (test infrastructure) -------------------------
+ * No counterpart in the reference.  The checker for the GPU constant
+ * gradient: each program evaluated in double precision with the same
+ * protected-function rules, F = (1/nlin) sum_n EF(p_n, y_n) with EF absolute
+ * (error_fn 0) or squared (1), and dF/d constant by a reverse sweep over a
+ * per-record tape of node values.  Ephemerals are given in double so that a
+ * finite-difference caller can perturb them by less than a float ulp. */
+static double d_value(int op, double a, double b, double c, int prot) {
+   switch (op) {
+   case OP_ADD: return a + b;
+   case OP_SUB: return a - b;
+   case OP_MULT: return a * b;
+   case OP_DIV: return (prot && b == 0.0) ? 1.0 : a / b;
+   case OP_MEAN: return (a + b) / 2.0;
+   case OP_MAX: return fmax(a, b);
+   case OP_MIN: return fmin(a, b);
+   case OP_POW: return pow(a, b);
+   case OP_ABS: return fabs(a);
+   case OP_POW2: return a * a;
+   case OP_POW3: return a * a * a;
+   case OP_POW4: return a * a * a * a;
+   case OP_POW5: return a * a * a * a * a;
+   case OP_NEG: return -a;
+   case OP_EXP: return exp(a);
+   case OP_EXP2: return exp2(a);
+   case OP_EXP10: return exp10(a);
+   case OP_SIN: return sin(a);
+   case OP_COS: return cos(a);
+   case OP_LOGISTIC: return 1.0 / (1.0 + exp(-a));
+   case OP_GAUSS: return exp(-a * a);
+   case OP_SQRT: return (prot && a < 0.0) ? 1.0 : sqrt(a);
+   case OP_LOG: return (prot && a < 1.0) ? 1.0 : log(a);
+   case OP_LOG2: return (prot && a < 1.0) ? 1.0 : log2(a);
+   case OP_LOG10: return (prot && a < 1.0) ? 1.0 : log10(a);
+   case OP_TAN: return tan(a);
+   case OP_IF_THEN_ELSE: return a != 0.0 ? b : c;
+   case OP_NOT: return a != 0.0 ? 0.0 : 1.0;
+   case OP_ROUND: return round(a);
+   case OP_CEIL: return ceil(a);
+   case OP_FLOOR: return floor(a);
+   case OP_STEP: return a >= 0.0 ? 1.0 : 0.0;
+   case OP_SIGN: return a > 0.0 ? 1.0 : (a < 0.0 ? -1.0 : 0.0);
+   case OP_AND: return (a != 0.0 && b != 0.0) ? 1.0 : 0.0;
+   case OP_OR: return (a != 0.0 || b != 0.0) ? 1.0 : 0.0;
+   case OP_XOR: return ((a != 0.0) != (b != 0.0)) ? 1.0 : 0.0;
+   case OP_GREATER: return a > b ? 1.0 : 0.0;
+   case OP_GREATEREQUAL: return a >= b ? 1.0 : 0.0;
+   case OP_LESS: return a < b ? 1.0 : 0.0;
+   case OP_LESSEQUAL: return a <= b ? 1.0 : 0.0;
+   case OP_EQUAL: return a == b ? 1.0 : 0.0;
+   case OP_NOTEQUAL: return a != b ? 1.0 : 0.0;
+   case OP_MOD: return fmod(a, b);
+   default: return NAN;   /* GAMMA and unknown ops are not differentiated */
+   }
+}
+
+static void d_partials(int op, double a, double b, double c, double v, int prot, double* da,
+                       double* db, double* dc) {
+   *da = 0.0; *db = 0.0; *dc = 0.0;
+   (void)c;
+   switch (op) {
+   case OP_ADD: *da = 1.0; *db = 1.0; break;
+   case OP_SUB: *da = 1.0; *db = -1.0; break;
+   case OP_MULT: *da = b; *db = a; break;
+   case OP_DIV: if (!(prot && b == 0.0)) { *da = 1.0 / b; *db = -v / b; } break;
+   case OP_MEAN: *da = 0.5; *db = 0.5; break;
+   case OP_MAX: if (a >= b) *da = 1.0; else *db = 1.0; break;
+   case OP_MIN: if (a <= b) *da = 1.0; else *db = 1.0; break;
+   case OP_POW: *da = b * v / a; *db = v * log(a); break;
+   case OP_MOD: *da = 1.0; *db = -trunc(a / b); break;
+   case OP_ABS: *da = a > 0.0 ? 1.0 : (a < 0.0 ? -1.0 : 0.0); break;
+   case OP_POW2: *da = 2.0 * a; break;
+   case OP_POW3: *da = 3.0 * a * a; break;
+   case OP_POW4: *da = 4.0 * a * a * a; break;
+   case OP_POW5: *da = 5.0 * a * a * a * a; break;
+   case OP_NEG: *da = -1.0; break;
+   case OP_EXP: *da = v; break;
+   case OP_EXP2: *da = v * log(2.0); break;
+   case OP_EXP10: *da = v * log(10.0); break;
+   case OP_SIN: *da = cos(a); break;
+   case OP_COS: *da = -sin(a); break;
+   case OP_LOGISTIC: *da = v * (1.0 - v); break;
+   case OP_GAUSS: *da = -2.0 * a * v; break;
+   case OP_SQRT: *da = (prot && a < 0.0) ? 0.0 : 0.5 / v; break;
+   case OP_LOG: *da = (prot && a < 1.0) ? 0.0 : 1.0 / a; break;
+   case OP_LOG2: *da = (prot && a < 1.0) ? 0.0 : 1.0 / (a * log(2.0)); break;
+   case OP_LOG10: *da = (prot && a < 1.0) ? 0.0 : 1.0 / (a * log(10.0)); break;
+   case OP_TAN: *da = 1.0 + v * v; break;
+   case OP_IF_THEN_ELSE: if (a != 0.0) *db = 1.0; else *dc = 1.0; break;
+   case OP_GAMMA: *da = NAN; break;
+   default: break;
+   }
+}
+
+int ppio_adjoint64(const ppio_config* c, const int32_t* phenotype, const double* ephemeral,
+                   const int32_t* size, int max_size, int n, int float_forward, double* fitness,
+                   double* grad) {
+   const int nlin = c->nlin, ncol = c->ncol, prot = c->protected_fns, fm = c->float_math;
+#ifdef _OPENMP
+   int nt = c->threads > 0 ? c->threads : omp_get_max_threads();
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nt)
+#endif
+   for (int i = 0; i < n; ++i) {
+      int sz = size[i];
+      double* g = grad + (size_t)i * max_size;
+      for (int k = 0; k < max_size; ++k) g[k] = 0.0;
+      if (sz <= 0 || sz > max_size) { fitness[i] = HUGE_VAL; continue; }
+      int* ops = (int*)malloc(sizeof(int) * (size_t)sz * 5);
+      double* val = (double*)malloc(sizeof(double) * (size_t)sz * 3);
+      int* sub = ops + sz;
+      int* ch = ops + 2 * sz;          /* ch[3k .. 3k+2]: children of position k */
+      double* lit = val;
+      double* v = val + sz;
+      double* adj = val + 2 * sz;
+      /* map tokens */
+      for (int k = 0; k < sz; ++k) {
+         int op = OP_INVALID;
+         double x = ephemeral[(size_t)i * max_size + k];
+         for (int q = 0; q < c->n_syms; ++q)
+            if (c->sym_values[q] == phenotype[(size_t)i * max_size + k]) {
+               op = c->sym_ops[q];
+               if (op == OP_LITERAL) x = (double)c->sym_literals[q];
+               break;
+            }
+         if (op == OP_ATTRIBUTE && !(x >= 0.0 && x < (double)ncol)) { op = OP_INVALID; }
+         ops[k] = op;
+         lit[k] = x;
+      }
+      /* structure (right to left): subtree sizes and children */
+      int depth = 0, bad = 0;
+      for (int k = sz - 1; k >= 0; --k) {
+         int ar = arity(ops[k]);
+         if (depth < ar) { bad = 1; break; }
+         depth = depth - ar + 1;
+         sub[k] = 1;
+         int cpos = k + 1;
+         for (int j = 0; j < 3; ++j) {
+            ch[3 * k + j] = -1;
+            if (j < ar) { ch[3 * k + j] = cpos; sub[k] += sub[cpos]; cpos += sub[cpos]; }
+         }
+      }
+      if (bad || depth != 1 || sub[0] != sz) {
+         fitness[i] = NAN;
+         for (int k = 0; k < sz; ++k) g[k] = NAN;
+         free(ops); free(val);
+         continue;
+      }
+      double F = 0.0;
+      int nonfin = 0;
+      for (int r = 0; r < nlin && !nonfin; ++r) {
+         const float* row = c->rows + (size_t)r * ncol;
+         for (int k = sz - 1; k >= 0; --k) {
+            int op = ops[k], ar = arity(op);
+            if (ar == 0) {
+               if (op == OP_ATTRIBUTE) v[k] = (double)row[(int)lit[k]];
+               else if (op == OP_INVALID) v[k] = NAN;
+               else v[k] = lit[k];
+            } else {
+               double a = v[ch[3 * k]], b = ar > 1 ? v[ch[3 * k + 1]] : 0.0,
+                      cc = ar > 2 ? v[ch[3 * k + 2]] : 0.0;
+               v[k] = float_forward ? (double)f_node(op, (float)a, (float)b, (float)cc, prot, fm)
+                                    : d_value(op, a, b, cc, prot);
+            }
+            if (float_forward && (ops[k] == OP_CONST || ops[k] == OP_LITERAL)) v[k] = (double)(float)v[k];
+         }
+         double y = (double)row[ncol - 1], d = v[0] - y;
+         double err = c->error_fn == 1 ? d * d : fabs(d);
+         if (float_forward) {
+            /* the float error and its non-finite rule, as the evaluator */
+            float fd = (float)v[0] - row[ncol - 1];
+            float fe = c->error_fn == 1 ? fd * fd : fabsf(fd);
+            if (isinf(fe) || isnan(fe)) { nonfin = 1; break; }
+         }
+         if (isinf(err) || isnan(err)) { nonfin = 1; break; }
+         F += err;
+         adj[0] = (c->error_fn == 1 ? 2.0 * d : (d > 0.0 ? 1.0 : (d < 0.0 ? -1.0 : 0.0))) / (double)nlin;
+         for (int k = 0; k < sz; ++k) {
+            int op = ops[k], ar = arity(op);
+            if (ar == 0) {
+               if (op == OP_CONST) g[k] += adj[k];
+               continue;
+            }
+            double a = v[ch[3 * k]], b = ar > 1 ? v[ch[3 * k + 1]] : 0.0,
+                   cc = ar > 2 ? v[ch[3 * k + 2]] : 0.0, pa, pb, pc;
+            d_partials(op, a, b, cc, v[k], prot, &pa, &pb, &pc);
+            /* a zero adjoint propagates zero (never 0 x inf = NaN) */
+            const int live = adj[k] != 0.0;
+            adj[ch[3 * k]] = live ? adj[k] * pa : 0.0;
+            if (ar > 1) adj[ch[3 * k + 1]] = live ? adj[k] * pb : 0.0;
+            if (ar > 2) adj[ch[3 * k + 2]] = live ? adj[k] * pc : 0.0;
+         }
+      }
+      if (nonfin) {
+         fitness[i] = HUGE_VAL;
+         for (int k = 0; k < sz; ++k) g[k] = 0.0;
+      } else {
+         fitness[i] = F / (double)nlin;
+      }
+      free(ops); free(val);
+   }
+   return 0;
+}

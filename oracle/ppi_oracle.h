@@ -59,6 +59,19 @@ int ppio_decode(const int32_t* rule_first, const int32_t* rule_count, const int3
                 const uint8_t* genomes, int n, int nb, int bg, int bc, float lo, float hi,
                 int max_size, int32_t* phenotype, float* ephemeral, int32_t* size);
 
+/* FP64 constant adjoint (no counterpart in the reference; the checker of the
+ * GPU constant gradient): fitness[i] = (1/nlin) sum_n EF(p_n, y_n) in double
+ * precision with EF absolute (error_fn 0) or squared (1), HUGE_VAL when an
+ * error is non-finite (gradient 0), NaN for a malformed program (gradient
+ * NaN); grad[i][k] = dF/d ephemeral[i][k] at CONST tokens, 0 elsewhere.
+ * ephemeral: n x max_size doubles.  float_forward = 1: the node values are
+ * the reference's float values (cfg->float_math selects the libm rounding, as
+ * in ppio_evaluate) and only the reverse sweep and the sums are double: the
+ * gradient of exactly the function the float evaluator computes. */
+int ppio_adjoint64(const ppio_config* cfg, const int32_t* phenotype, const double* ephemeral,
+                   const int32_t* size, int max_size, int n, int float_forward, double* fitness,
+                   double* grad);
+
 #ifdef __cplusplus
 }
 #endif

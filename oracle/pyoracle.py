@@ -64,6 +64,9 @@ def lib():
                                     C.c_int, C.c_float, _fp]
         L.ppio_predict.argtypes = [C.POINTER(_Cfg), _ip, _fp, C.c_int, _fp]
         L.ppio_best_index.argtypes = [_fp, C.c_int]
+        _dp = C.POINTER(C.c_double)
+        L.ppio_adjoint64.argtypes = [C.POINTER(_Cfg), _ip, _dp, _ip, C.c_int, C.c_int, C.c_int, _dp,
+                                     _dp]
         L.ppio_decode.argtypes = [_ip, _ip, _ip, _ip, C.c_int, C.c_int, C.c_int, _up, C.c_int,
                                   C.c_int, C.c_int, C.c_int, C.c_float, C.c_float, C.c_int, _ip,
                                   _fp, _ip]
@@ -96,6 +99,22 @@ class Oracle:
                                  _i(sz), mps, n, alpha, _f(out))
         assert rc == 0
         return out
+
+    def adjoint64(self, phenotype, ephemeral, size, float_forward=False):
+        """FP64 fitness and d(fitness)/d(ephemeral) (ppio_adjoint64); ephemeral
+        is taken in double so a finite-difference caller can perturb it finely.
+        float_forward: node values in the reference's float semantics."""
+        ph = np.ascontiguousarray(phenotype, np.int32)
+        ep = np.ascontiguousarray(ephemeral, np.float64)
+        sz = np.ascontiguousarray(size, np.int32)
+        n, mps = ph.shape
+        fit = np.empty(n, np.float64)
+        grad = np.empty((n, mps), np.float64)
+        dp = C.POINTER(C.c_double)
+        assert lib().ppio_adjoint64(C.byref(self.cfg), _i(ph), ep.ctypes.data_as(dp), _i(sz), mps, n,
+                                    int(float_forward), fit.ctypes.data_as(dp),
+                                    grad.ctypes.data_as(dp)) == 0
+        return fit, grad
 
     def predict(self, phenotype, ephemeral, size):
         ph = np.ascontiguousarray(phenotype, np.int32)

@@ -67,6 +67,12 @@ struct ppi_gpu {
    size_t frames_cap = 0;
    float last_ms = 0.0f;
    int last_launches = 0;
+   // constant adjoint (allocated on first use)
+   uint4* d_adj_code = nullptr;
+   int2* d_adj_meta = nullptr;
+   float* d_grad = nullptr;
+   int* d_adj_stats = nullptr;   // max rows, max constants, work queue
+   int* h_adj_stats = nullptr;
 };
 
 namespace {
@@ -99,6 +105,8 @@ void free_all(ppi_gpu* h) {
    cudaFree(h->d_genomes); cudaFree(h->d_frames);
    free_decode_tables(&h->dec);
    cudaFreeHost(h->h_fit); cudaFreeHost(h->h_best); cudaFreeHost(h->h_status);
+   cudaFree(h->d_adj_code); cudaFree(h->d_adj_meta); cudaFree(h->d_grad); cudaFree(h->d_adj_stats);
+   cudaFreeHost(h->h_adj_stats);
    if (h->ev0) cudaEventDestroy(h->ev0);
    if (h->ev1) cudaEventDestroy(h->ev1);
    if (h->evm) cudaEventDestroy(h->evm);
@@ -383,6 +391,64 @@ ppi_status ppi_gpu_predict(ppi_gpu* h, const int32_t* ph, const float* eph, int3
    PPI_CUDA(h, cudaEventRecord(h->ev1, h->stream));
    PPI_CUDA(h, cudaMemcpyAsync(out, h->d_pred, (size_t)h->nlin * 4, cudaMemcpyDeviceToHost, h->stream));
    PPI_CUDA(h, cudaStreamSynchronize(h->stream));
+   cudaEventElapsedTime(&h->last_ms, h->ev0, h->ev1);
+   h->last_launches = 2;
+   return PPI_OK;
+}
+
+ppi_status ppi_gpu_constant_gradient(ppi_gpu* h, const int32_t* ph, const float* eph,
+                                     const int32_t* size, int32_t n, float* gradient) {
+   ppi_status s = check_ready(h, n);
+   if (s != PPI_OK) return s;
+   if (!ph || !eph || !size || !gradient) return fail(h, PPI_ERR_INVALID_ARGUMENT, "null argument");
+   if (h->cfg.reduce_max || (h->cfg.error_fn != PPI_EF_ABS && h->cfg.error_fn != PPI_EF_SQUARED))
+      return fail(h, PPI_ERR_UNSUPPORTED,
+                  "constant gradients need the sum reduction with the absolute or squared error");
+   PPI_CUDA(h, cudaSetDevice(h->device));
+   const size_t pop = (size_t)h->cfg.population_size, ms = (size_t)h->cfg.max_size;
+   const int stride = adjoint_code_stride(h->cfg.max_size);
+   if (!h->d_adj_code) {
+      PPI_CUDA(h, dalloc(&h->d_adj_code, pop * stride));
+      PPI_CUDA(h, dalloc(&h->d_adj_meta, pop));
+      PPI_CUDA(h, dalloc(&h->d_grad, pop * ms));
+      PPI_CUDA(h, dalloc(&h->d_adj_stats, 4));
+      PPI_CUDA(h, cudaMallocHost(reinterpret_cast<void**>(&h->h_adj_stats), 4 * sizeof(int)));
+   }
+   cudaStream_t st = h->stream;
+   PPI_CUDA(h, cudaMemcpyAsync(h->d_ph, ph, (size_t)n * ms * 4, cudaMemcpyHostToDevice, st));
+   PPI_CUDA(h, cudaMemcpyAsync(h->d_eph, eph, (size_t)n * ms * 4, cudaMemcpyHostToDevice, st));
+   PPI_CUDA(h, cudaMemcpyAsync(h->d_size, size, (size_t)n * 4, cudaMemcpyHostToDevice, st));
+   PPI_CUDA(h, cudaMemsetAsync(h->d_adj_stats, 0, 4 * sizeof(int), st));
+   AdjointTranslateArgs t{};
+   t.phenotype = h->d_ph; t.ephemeral = h->d_eph; t.size = h->d_size; t.n = n;
+   t.max_size = h->cfg.max_size; t.ncol = h->ncol;
+   t.lut = h->d_lut; t.lut_min = h->lut_min; t.lut_len = h->lut_len;
+   t.code = h->d_adj_code; t.code_stride = stride; t.meta = h->d_adj_meta; t.work = h->d_work;
+   t.max_rows = h->d_adj_stats; t.max_consts = h->d_adj_stats + 1;
+   PPI_CUDA(h, launch_adjoint_translate(t, st));
+   PPI_CUDA(h, cudaMemcpyAsync(h->h_adj_stats, h->d_adj_stats, 2 * sizeof(int), cudaMemcpyDeviceToHost, st));
+   PPI_CUDA(h, cudaStreamSynchronize(st));
+   // tape rows of the longest program decide the block: the largest of 128,
+   // 64, 32 threads (4 records each) whose tile fits in 96 KB, else the one
+   // that fits in 200 KB
+   const int rows = std::max(1, h->h_adj_stats[0]), nconst = std::max(1, h->h_adj_stats[1]);
+   int P = 128;
+   while (P > 32 && adjoint_smem_bytes(stride, nconst, rows, P) > 96 * 1024) P /= 2;
+   const size_t smem = adjoint_smem_bytes(stride, nconst, rows, P);
+   if (smem > 200 * 1024) return fail(h, PPI_ERR_UNSUPPORTED, "program tape too long for shared memory");
+   int per_sm = 0;
+   if (adjoint_occupancy(h->cfg.math, P, smem, &per_sm) != cudaSuccess || per_sm < 1)
+      return fail(h, PPI_ERR_UNSUPPORTED, "adjoint kernel does not fit on an SM");
+   AdjointArgs a{};
+   a.data = h->d_data; a.nlin = h->nlin; a.ncol = h->ncol; a.ld = h->ld;
+   a.code = h->d_adj_code; a.code_stride = stride; a.meta = h->d_adj_meta;
+   a.n = n; a.max_size = h->cfg.max_size; a.ef = h->cfg.error_fn; a.prot = h->cfg.protected_fns ? 1 : 0;
+   a.max_consts = nconst; a.grad = h->d_grad; a.queue = reinterpret_cast<unsigned*>(h->d_adj_stats + 2);
+   PPI_CUDA(h, cudaEventRecord(h->ev0, st));
+   PPI_CUDA(h, launch_adjoint(h->cfg.math, a, P, std::max(1, std::min(n, per_sm * h->sm_count)), smem, st));
+   PPI_CUDA(h, cudaEventRecord(h->ev1, st));
+   PPI_CUDA(h, cudaMemcpyAsync(gradient, h->d_grad, (size_t)n * ms * 4, cudaMemcpyDeviceToHost, st));
+   PPI_CUDA(h, cudaStreamSynchronize(st));
    cudaEventElapsedTime(&h->last_ms, h->ev0, h->ev1);
    h->last_launches = 2;
    return PPI_OK;

@@ -361,6 +361,46 @@ struct PredictArgs {
    float* out;
 };
 
+// ---------------------------------------------------------------------------
+// Constant adjoint (adjoint.cu).
+enum : int { kAdjInvalid = 0, kAdjValid = 1, kAdjUnsupported = 2 };
+// Most ephemeral constants of one program the adjoint differentiates.
+constexpr int kAdjMaxConsts = 32;
+// uint4 entries of one program's tape code: header, two per operator, one
+// per constant or literal.
+inline int adjoint_code_stride(int max_size) { return 1 + 3 * max_size; }
+
+struct AdjointTranslateArgs {
+   const int32_t* phenotype;
+   const float* ephemeral;
+   const int32_t* size;
+   int n, max_size, ncol;
+   const int2* lut;
+   int lut_min, lut_len;
+   uint4* code;                // program i at code + i * code_stride
+   int code_stride;
+   int2* meta;                 // {kAdj* | rows << 8, code length}
+   uint2* work;                // n x 2 max_size scratch
+   int* max_rows;              // over the population (atomicMax)
+   int* max_consts;
+};
+
+struct AdjointArgs {
+   const float* data;          // column-major, column c at data + c * ld
+   int nlin, ncol, ld;
+   const uint4* code;
+   int code_stride;
+   const int2* meta;
+   int n, max_size, ef, prot, max_consts;
+   float* grad;                // n x max_size
+   unsigned* queue;
+};
+
+cudaError_t launch_adjoint_translate(const AdjointTranslateArgs& a, cudaStream_t s);
+cudaError_t launch_adjoint(int math, const AdjointArgs& a, int block, int grid, size_t smem, cudaStream_t s);
+cudaError_t adjoint_occupancy(int math, int block, size_t smem, int* per_sm);
+size_t adjoint_smem_bytes(int code_stride, int max_consts, int rows, int block);
+
 // Evaluator launch geometry: lanes, block size P, records per thread R, and
 // for the main and the wide pass the row budget, dynamic shared memory and a
 // one-wave persistent grid.  The main pass runs the programs whose columns

@@ -98,6 +98,7 @@ def load_library():
     L.ppi_gpu_last_launch_count.argtypes = [C.c_void_p]
     L.ppi_gpu_last_stage_ms.argtypes = [C.c_void_p, _fp, _fp]
     L.ppi_gpu_lanes.argtypes = [C.c_void_p]
+    L.ppi_gpu_constant_gradient.argtypes = [C.c_void_p, _ip, _fp, _ip, C.c_int32, _fp]
     L.ppi_batch_create.argtypes = [C.POINTER(Config), C.c_int32, C.POINTER(BatchPopulation),
                                    C.POINTER(C.c_void_p)]
     L.ppi_batch_destroy.argtypes = [C.c_void_p]
@@ -201,6 +202,17 @@ class Evaluator:
         """Device pointers (ints) in, queued on `stream`; no synchronisation."""
         self._check(self._L.ppi_gpu_evaluate_device(self._h, d_ph, d_eph, d_size, n, alpha,
                                                     d_fit, d_best, stream))
+
+    def constant_gradient(self, phenotype, ephemeral, size):
+        """d(fitness)/d(ephemeral[i][k]) at every CONST token (0 elsewhere)."""
+        ph = np.ascontiguousarray(phenotype, np.int32)
+        ep = np.ascontiguousarray(ephemeral, np.float32)
+        sz = np.ascontiguousarray(size, np.int32)
+        n = len(sz)
+        assert ph.shape == (n, self.max_size) and ep.shape == (n, self.max_size)
+        grad = np.empty((n, self.max_size), np.float32)
+        self._check(self._L.ppi_gpu_constant_gradient(self._h, _i(ph), _f(ep), _i(sz), n, _f(grad)))
+        return grad
 
     def predict(self, phenotype, ephemeral, size):
         ph = np.ascontiguousarray(phenotype, np.int32)

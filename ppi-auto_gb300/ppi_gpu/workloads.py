@@ -207,3 +207,36 @@ def uneven_batch(seed=11, n_pops=64, pop_range=(256, 30000), rec_range=(100, 1_0
                          size=lengths.astype(np.int32), strategy="PDP", error_fn="abs",
                          protected=True))
     return g, pops
+
+
+def adjoint(seed=21, nlin=100_000, population=10_000, max_size=64, mean_len=20):
+    """Constant-adjoint configuration: nlin records x 8 N(0,1) features, y = a
+    random depth-5 expression (sin/exp/log/*,/) + N(0, 0.05); programs are
+    random valid prefix trees over + - * / sin exp log (geometric lengths, mean
+    20, 3..max_size) whose leaves are attributes and 1-8 ephemeral constants
+    uniform in [-2, 2]; EF squared error, sum.  Returns (grammar, rows,
+    phenotype, ephemeral, size)."""
+    rng = np.random.default_rng(seed)
+    g = G.load(os.path.join(GRAMMARS, "config4_adjoint.bnf"))
+    X = rng.normal(0.0, 1.0, (nlin, 8))
+    y = _random_target(rng, X) + rng.normal(0.0, 0.05, nlin)
+    rows = np.concatenate([X, y[:, None]], 1).astype(np.float32)
+    S = g.symbols
+    lengths = np.clip(rng.geometric(1.0 / mean_len, population), 3, max_size)
+    ph, ep = random_programs(rng, lengths, 8, g, p_unary=0.25)
+    attr, const = S["T_ATTRIBUTE"], S["T_CONST"]
+    size = lengths.astype(np.int32)
+    # exactly k = 1..8 constant leaves (as many as the program has leaves)
+    for i in range(population):
+        leaves = np.flatnonzero((ph[i, :size[i]] == attr) | (ph[i, :size[i]] == const))
+        k = min(len(leaves), int(rng.integers(1, 9)))
+        pick = rng.choice(leaves, k, replace=False)
+        ph[i, leaves] = attr
+        ep[i, leaves] = rng.integers(0, 8, len(leaves)).astype(np.float32)
+        ph[i, pick] = const
+        ep[i, pick] = rng.uniform(-2.0, 2.0, k).astype(np.float32)
+    phf = np.zeros((population, max_size), np.int32)
+    epf = np.zeros((population, max_size), np.float32)
+    phf[:, :ph.shape[1]] = ph
+    epf[:, :ep.shape[1]] = ep
+    return g, rows, phf, epf, size
