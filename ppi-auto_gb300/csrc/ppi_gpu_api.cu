@@ -71,8 +71,11 @@ struct ppi_gpu {
    uint4* d_adj_code = nullptr;
    int2* d_adj_meta = nullptr;
    float* d_grad = nullptr;
-   int* d_adj_stats = nullptr;   // max rows, max constants, work queue
+   int* d_adj_stats = nullptr;   // max rows, max constants, work queues of the two passes
    int* h_adj_stats = nullptr;
+   int* d_adj_order = nullptr;
+   std::vector<int2> h_adj_meta;
+   std::vector<int> h_adj_order;
 };
 
 namespace {
@@ -106,6 +109,7 @@ void free_all(ppi_gpu* h) {
    free_decode_tables(&h->dec);
    cudaFreeHost(h->h_fit); cudaFreeHost(h->h_best); cudaFreeHost(h->h_status);
    cudaFree(h->d_adj_code); cudaFree(h->d_adj_meta); cudaFree(h->d_grad); cudaFree(h->d_adj_stats);
+   cudaFree(h->d_adj_order);
    cudaFreeHost(h->h_adj_stats);
    if (h->ev0) cudaEventDestroy(h->ev0);
    if (h->ev1) cudaEventDestroy(h->ev1);
@@ -426,31 +430,64 @@ ppi_status ppi_gpu_constant_gradient(ppi_gpu* h, const int32_t* ph, const float*
    t.code = h->d_adj_code; t.code_stride = stride; t.meta = h->d_adj_meta; t.work = h->d_work;
    t.max_rows = h->d_adj_stats; t.max_consts = h->d_adj_stats + 1;
    PPI_CUDA(h, launch_adjoint_translate(t, st));
+   h->h_adj_meta.resize((size_t)n);
    PPI_CUDA(h, cudaMemcpyAsync(h->h_adj_stats, h->d_adj_stats, 2 * sizeof(int), cudaMemcpyDeviceToHost, st));
+   PPI_CUDA(h, cudaMemcpyAsync(h->h_adj_meta.data(), h->d_adj_meta, (size_t)n * sizeof(int2),
+                               cudaMemcpyDeviceToHost, st));
    PPI_CUDA(h, cudaStreamSynchronize(st));
-   // tape rows of the longest program decide the block: the largest of 128,
-   // 64, 32 threads (4 records each) whose tile fits in 96 KB, else the one
-   // that fits in 200 KB
-   const int rows = std::max(1, h->h_adj_stats[0]), nconst = std::max(1, h->h_adj_stats[1]);
-   int P = 128;
-   while (P > 32 && adjoint_smem_bytes(stride, nconst, rows, P) > 96 * 1024) P /= 2;
-   const size_t smem = adjoint_smem_bytes(stride, nconst, rows, P);
-   if (smem > 200 * 1024) return fail(h, PPI_ERR_UNSUPPORTED, "program tape too long for shared memory");
-   int per_sm = 0;
-   if (adjoint_occupancy(h->cfg.math, P, smem, &per_sm) != cudaSuccess || per_sm < 1)
-      return fail(h, PPI_ERR_UNSUPPORTED, "adjoint kernel does not fit on an SM");
+   // Two passes over 128-thread CTAs (4 records each): the programs whose
+   // tape fits the tile at the kernel's best occupancy, then the rest with a
+   // tile for the longest tape (a narrower CTA when 128 threads do not fit).
+   const int rows_max = std::max(1, h->h_adj_stats[0]), nconst = std::max(1, h->h_adj_stats[1]);
+   auto occ = [&](int P, int rows) {
+      int per_sm = 0;
+      const size_t smem = adjoint_smem_bytes(stride, nconst, rows, P);
+      if (smem > 200 * 1024 || adjoint_occupancy(h->cfg.math, h->opset, P, smem, &per_sm) != cudaSuccess)
+         return 0;
+      return per_sm;
+   };
+   const int P1 = 128;
+   const int top = occ(P1, 1);
+   if (top < 1) return fail(h, PPI_ERR_UNSUPPORTED, "adjoint kernel does not fit on an SM");
+   int rows1 = 1;
+   while (rows1 < rows_max && occ(P1, rows1 + 1) >= top) ++rows1;
+   int P2 = 128;
+   while (P2 > 32 && occ(P2, rows_max) < 1) P2 /= 2;
+   if (occ(P2, rows_max) < 1) return fail(h, PPI_ERR_UNSUPPORTED, "program tape too long for shared memory");
+   h->h_adj_order.clear();
+   for (int i = 0; i < n; ++i)
+      if ((h->h_adj_meta[i].x >> 8) <= rows1) h->h_adj_order.push_back(i);
+   const int n1 = (int)h->h_adj_order.size();
+   for (int i = 0; i < n; ++i)
+      if ((h->h_adj_meta[i].x >> 8) > rows1) h->h_adj_order.push_back(i);
+   if (!h->d_adj_order) PPI_CUDA(h, dalloc(&h->d_adj_order, pop));
+   PPI_CUDA(h, cudaMemcpyAsync(h->d_adj_order, h->h_adj_order.data(), (size_t)n * sizeof(int),
+                               cudaMemcpyHostToDevice, st));
    AdjointArgs a{};
    a.data = h->d_data; a.nlin = h->nlin; a.ncol = h->ncol; a.ld = h->ld;
    a.code = h->d_adj_code; a.code_stride = stride; a.meta = h->d_adj_meta;
-   a.n = n; a.max_size = h->cfg.max_size; a.ef = h->cfg.error_fn; a.prot = h->cfg.protected_fns ? 1 : 0;
-   a.max_consts = nconst; a.grad = h->d_grad; a.queue = reinterpret_cast<unsigned*>(h->d_adj_stats + 2);
+   a.max_size = h->cfg.max_size; a.ef = h->cfg.error_fn; a.prot = h->cfg.protected_fns ? 1 : 0;
+   a.max_consts = nconst; a.grad = h->d_grad;
    PPI_CUDA(h, cudaEventRecord(h->ev0, st));
-   PPI_CUDA(h, launch_adjoint(h->cfg.math, a, P, std::max(1, std::min(n, per_sm * h->sm_count)), smem, st));
+   h->last_launches = 1;
+   if (n1 > 0) {
+      a.order = h->d_adj_order; a.n_items = n1; a.queue = reinterpret_cast<unsigned*>(h->d_adj_stats + 2);
+      PPI_CUDA(h, launch_adjoint(h->cfg.math, h->opset, a, P1, std::max(1, std::min(n1, top * h->sm_count)),
+                                 adjoint_smem_bytes(stride, nconst, rows1, P1), st));
+      ++h->last_launches;
+   }
+   if (n1 < n) {
+      const int per2 = occ(P2, rows_max);
+      a.order = h->d_adj_order + n1; a.n_items = n - n1;
+      a.queue = reinterpret_cast<unsigned*>(h->d_adj_stats + 3);
+      PPI_CUDA(h, launch_adjoint(h->cfg.math, h->opset, a, P2, std::max(1, std::min(n - n1, per2 * h->sm_count)),
+                                 adjoint_smem_bytes(stride, nconst, rows_max, P2), st));
+      ++h->last_launches;
+   }
    PPI_CUDA(h, cudaEventRecord(h->ev1, st));
    PPI_CUDA(h, cudaMemcpyAsync(gradient, h->d_grad, (size_t)n * ms * 4, cudaMemcpyDeviceToHost, st));
    PPI_CUDA(h, cudaStreamSynchronize(st));
    cudaEventElapsedTime(&h->last_ms, h->ev0, h->ev1);
-   h->last_launches = 2;
    return PPI_OK;
 }
 

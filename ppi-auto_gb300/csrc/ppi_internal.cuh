@@ -391,14 +391,17 @@ struct AdjointArgs {
    const uint4* code;
    int code_stride;
    const int2* meta;
-   int n, max_size, ef, prot, max_consts;
+   int max_size, ef, prot, max_consts;
+   const int* order;           // programs of this pass (nullptr: 0 .. n_items-1)
+   int n_items;
    float* grad;                // n x max_size
    unsigned* queue;
 };
 
 cudaError_t launch_adjoint_translate(const AdjointTranslateArgs& a, cudaStream_t s);
-cudaError_t launch_adjoint(int math, const AdjointArgs& a, int block, int grid, size_t smem, cudaStream_t s);
-cudaError_t adjoint_occupancy(int math, int block, size_t smem, int* per_sm);
+cudaError_t launch_adjoint(int math, int opset, const AdjointArgs& a, int block, int grid, size_t smem,
+                           cudaStream_t s);
+cudaError_t adjoint_occupancy(int math, int opset, int block, size_t smem, int* per_sm);
 size_t adjoint_smem_bytes(int code_stride, int max_consts, int rows, int block);
 
 // Evaluator launch geometry: lanes, block size P, records per thread R, and
