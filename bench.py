@@ -126,19 +126,21 @@ def profile_traffic(workload):
     return profile_value("eval_kernel_" + workload, "traffic_bytes_per_launch")
 
 
-def cpu_sample(wl, ph, eph, sz, budget_s, threads=0, chunk=200):
+def cpu_sample(wl, ph, eph, sz, budget_s, threads=0, chunk=0):
     """Oracle port (OpenMP over programs) on the first programs of the
     population, all records, until budget_s of work: (GPop/s, programs, cores)."""
     from oracle import pyoracle
     pyoracle.build()
     o = pyoracle.Oracle(wl.rows, wl.grammar.symbol_table_arrays(), wl.error_fn, wl.cost,
                         wl.reduce_max, wl.protected, False, threads)
+    cores = threads if threads > 0 else (os.cpu_count() or 1)
+    chunk = chunk or 2 * cores
     done, ops, t = 0, 0, 0.0
     while done < len(sz) and (t < budget_s or done == 0):
         k = min(chunk, len(sz) - done)
         t0 = time.perf_counter()
-        o.evaluate(ph[done:done + k], eph[done:done + k], sz[done:done + k], "PDP",
-                   min(wl.nlin, 1024), 1e-6)
+        o.evaluate(ph[done:done + k], eph[done:done + k], sz[done:done + k], wl.strategy,
+                   1 if wl.strategy == "PP" else min(wl.nlin, 1024), 1e-6)
         t += time.perf_counter() - t0
         ops += int(sz[done:done + k].sum()) * wl.nlin
         done += k
@@ -519,7 +521,12 @@ def run_polynomial(args):
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
-    wl = workloads.polynomial(seed=1234 + rank, nlin=args.records, population=args.population)
+    if args.workload == "polynomial":
+        wl = workloads.polynomial(seed=1234 + rank, nlin=args.records, population=args.population)
+    elif args.workload == "iris":
+        wl = workloads.iris_shaped(seed=99 + rank, population=args.population)
+    else:
+        wl = workloads.streaming(seed=7 + rank, nlin=args.records, population=args.population)
     ev = ppi_gpu.Evaluator(wl.grammar.symbol_table_arrays(), wl.max_size, wl.population,
                            wl.strategy, 0, wl.error_fn, wl.cost, wl.reduce_max, wl.protected,
                            args.math, device=local)
@@ -618,7 +625,7 @@ def run_polynomial(args):
         "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(total_s * 1e3 / args.steps, 4), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
-        "config": dict(wl.describe(), lanes=min(wl.nlin, 1024), math=args.math,
+        "config": dict(wl.describe(), lanes=ev.lanes, math=args.math,
                        sum_size=int(sz.sum()), ops_per_step=ops_per_step,
                        l2="256 MiB buffer written between steps, outside the timed events",
                        decode_ms=round(decode_ms, 3)),
@@ -650,7 +657,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--math", default="fast", choices=["fast", "parity", "native"])
-    ap.add_argument("--workload", default="uneven", choices=["uneven", "polynomial", "adjoint"])
+    ap.add_argument("--workload", default="uneven",
+                    choices=["uneven", "polynomial", "iris", "stream", "adjoint"])
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--cpu-fraction", type=float, default=0.015,
                     help="uneven batch: share of every population timed on the CPU")
@@ -663,7 +671,11 @@ def main():
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
     if args.impl == "reference":
         return run_reference(args)
-    if args.workload == "polynomial":
+    if args.workload in ("polynomial", "iris", "stream"):
+        if args.workload == "stream" and args.records == 100_000:
+            args.records = 4_000_000
+        if args.workload == "iris" and args.population == 30_000:
+            args.population = 1000
         return run_polynomial(args)
     if args.workload == "adjoint":
         return run_adjoint(args)

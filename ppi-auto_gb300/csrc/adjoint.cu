@@ -19,7 +19,8 @@
 // Evaluation (one CTA per program, persistent work queue): for each tile of
 // T = P x 4 records the forward sweep is recomputed into the tape (no
 // per-record tape outlives its tile), then the reverse sweep accumulates each
-// constant's gradient in a per-thread double partial.  A thread reads and
+// constant's gradient in a per-thread float partial, added into a double sum
+// every 32 tiles (few double operations, short float sums).  A thread reads and
 // writes only its own 4 positions of every row, so the sweeps need no
 // barriers.  Attributes and targets are read from global memory (the
 // dataset stays in L2 at the sizes this serves).  Any non-finite error makes
@@ -287,16 +288,18 @@ __device__ __forceinline__ void adj_load(uint32_t d, const float* s_rows, int T,
 }
 
 // Deliver an operand's adjoints: its tape row `dst`, a constant's partial
-// sum, or nowhere (attributes, literals).
+// sum (this thread's float partial, flushed into a double one every
+// kAdjFlush tiles), or nowhere (attributes, literals).
+constexpr int kAdjFlush = 32;
 __device__ __forceinline__ void adj_store(uint32_t d, uint32_t dst, const float (&x)[4], float* s_rows, int T,
-                                          int tid, int P, const uint4* s_tab, double* s_part) {
+                                          int tid, int P, const uint4* s_tab, float* s_part) {
    const uint32_t kind = opd_kind(d);
    if (kind == kOpdRow) {
       if (dst != kAdjNoRow)
          *reinterpret_cast<float4*>(s_rows + (size_t)dst * T + tid * 4) = make_float4(x[0], x[1], x[2], x[3]);
    } else if (kind == kOpdConst) {
       const uint32_t slot = s_tab[opd_val(d)].z;
-      s_part[slot * P + tid] += (double)((x[0] + x[1]) + (x[2] + x[3]));
+      s_part[slot * P + tid] += (x[0] + x[1]) + (x[2] + x[3]);
    }
 }
 
@@ -378,7 +381,7 @@ __device__ __forceinline__ void adj_forward(const uint4* s_code, int ninstr, flo
 
 template <int MATH, int OPSET>
 __device__ __forceinline__ void adj_reverse(const uint4* s_code, int ninstr, float* s_rows, int T, int tid,
-                                            int P, const uint4* s_tab, double* s_part, const float* data,
+                                            int P, const uint4* s_tab, float* s_part, const float* data,
                                             int ld, int base, int nlin, int prot) {
    for (int j = ninstr - 1; j >= 0; --j) {
       const uint4 i0 = s_code[1 + 2 * j];
@@ -437,9 +440,9 @@ __global__ void __launch_bounds__(128) adjoint_kernel(const AdjointArgs a) {
    __shared__ int s_prog, s_bad;
    const int P = blockDim.x, tid = threadIdx.x, T = P * kAdjR;
    uint4* s_code = reinterpret_cast<uint4*>(smem_raw);
-   double* s_part = reinterpret_cast<double*>(smem_raw + (size_t)a.code_stride * sizeof(uint4));
-   float* s_rows = reinterpret_cast<float*>(reinterpret_cast<unsigned char*>(s_part) +
-                                            (size_t)a.max_consts * P * sizeof(double));
+   double* s_sum = reinterpret_cast<double*>(smem_raw + (size_t)a.code_stride * sizeof(uint4));
+   float* s_part = reinterpret_cast<float*>(s_sum + (size_t)a.max_consts * P);
+   float* s_rows = s_part + (size_t)a.max_consts * P;
    const float inv_n = 1.0f / (float)a.nlin;
    for (;;) {
       if (tid == 0) {
@@ -467,7 +470,11 @@ __global__ void __launch_bounds__(128) adjoint_kernel(const AdjointArgs a) {
       const int m = ninstr;   // row of the root's adjoint
       const uint32_t root = hdr.w;
       const uint4* s_tab = s_code + 1 + 2 * ninstr;
-      for (int q = 0; q < nconst; ++q) s_part[q * P + tid] = 0.0;
+      for (int q = 0; q < nconst; ++q) {
+         s_sum[q * P + tid] = 0.0;
+         s_part[q * P + tid] = 0.0f;
+      }
+      int tiles = 0;
       for (int base = 0; base < a.nlin; base += T) {
          adj_forward<MATH, OPSET>(s_code, ninstr, s_rows, T, tid, s_tab, a.data, a.ld, base, a.prot);
          // prediction, error derivative, the root's adjoint
@@ -489,12 +496,19 @@ __global__ void __launch_bounds__(128) adjoint_kernel(const AdjointArgs a) {
          if (bad) s_bad = 1;
          if (opd_kind(root) == kOpdConst) {
             const uint32_t slot = s_tab[opd_val(root)].z;
-            s_part[slot * P + tid] += (double)((e1[0] + e1[1]) + (e1[2] + e1[3]));
+            s_part[slot * P + tid] += (e1[0] + e1[1]) + (e1[2] + e1[3]);
          }
          if (ninstr > 0)
             *reinterpret_cast<float4*>(s_rows + (size_t)m * T + tid * 4) = make_float4(e1[0], e1[1], e1[2], e1[3]);
          adj_reverse<MATH, OPSET>(s_code, ninstr, s_rows, T, tid, P, s_tab, s_part, a.data, a.ld, base,
                                   a.nlin, a.prot);
+         if (++tiles == kAdjFlush || base + T >= a.nlin) {
+            for (int q = 0; q < nconst; ++q) {
+               s_sum[q * P + tid] += (double)s_part[q * P + tid];
+               s_part[q * P + tid] = 0.0f;
+            }
+            tiles = 0;
+         }
       }
       __syncthreads();
       // reduce the partials of each constant and write the gradient at its token
@@ -503,7 +517,7 @@ __global__ void __launch_bounds__(128) adjoint_kernel(const AdjointArgs a) {
       for (int t = 0; t < ntab; ++t) {
          const uint4 e = s_tab[t];
          if (e.z == ~0u) continue;
-         double* pp = s_part + e.z * P;
+         double* pp = s_sum + e.z * P;
          for (int st = P >> 1; st > 0; st >>= 1) {
             if (tid < st) pp[tid] += pp[tid + st];
             __syncthreads();
@@ -522,7 +536,7 @@ cudaError_t launch_adjoint_translate(const AdjointTranslateArgs& a, cudaStream_t
 }
 
 size_t adjoint_smem_bytes(int code_stride, int max_consts, int rows, int block) {
-   return (size_t)code_stride * sizeof(uint4) + (size_t)max_consts * block * sizeof(double) +
+   return (size_t)code_stride * sizeof(uint4) + (size_t)max_consts * block * (sizeof(double) + sizeof(float)) +
           (size_t)rows * block * kAdjR * sizeof(float);
 }
 
