@@ -105,6 +105,20 @@ class ClockSampler:
                 "samples": len(self.rows)}
 
 
+def aggregate(times, counts, device, world):
+    """Weak-scaling aggregation over ranks, the benchmark's only collective:
+    the slowest rank's times and the sum of all ranks' work."""
+    if world == 1:
+        return [float(t) for t in times], [float(c) for c in counts]
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(x) for x in times], dtype=torch.float64, device=device)
+    c = torch.tensor([float(x) for x in counts], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.all_reduce(c, op=dist.ReduceOp.SUM)
+    return t.tolist(), c.tolist()
+
+
 def measured_peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     return json.load(open(p)) if os.path.exists(p) else {}
@@ -362,15 +376,7 @@ def run_batch(args):
 
     total_s = sum(step_ms) / 1e3
     plain_s = sum(plain_ms) / 1e3
-    tot = torch.tensor([total_s, e2e_s, plain_s, work], dtype=torch.float64, device=dev)
-    if world > 1:
-        mx = tot.clone()
-        torch.distributed.all_reduce(mx[:3], op=torch.distributed.ReduceOp.MAX)
-        sm = tot.clone()
-        torch.distributed.all_reduce(sm[3:], op=torch.distributed.ReduceOp.SUM)
-        total_s, e2e_s, plain_s, all_ops = float(mx[0]), float(mx[1]), float(mx[2]), float(sm[3])
-    else:
-        all_ops = work
+    (total_s, e2e_s, plain_s), (all_ops,) = aggregate([total_s, e2e_s, plain_s], [work], dev, world)
     if rank != 0:
         return 0
     value = all_ops * args.steps / total_s / 1e9
@@ -598,15 +604,7 @@ def run_polynomial(args):
     e2e_s = time.perf_counter() - t0
     assert np.array_equal(fit_e2e.view(np.int32), fit_host.view(np.int32))
 
-    tot = torch.tensor([total_s, e2e_s, float(ops_per_step)], dtype=torch.float64, device=dev)
-    if world > 1:
-        mx = tot.clone()
-        torch.distributed.all_reduce(mx[:2], op=torch.distributed.ReduceOp.MAX)
-        sm = tot.clone()
-        torch.distributed.all_reduce(sm[2:], op=torch.distributed.ReduceOp.SUM)
-        total_s, e2e_s, all_ops = float(mx[0]), float(mx[1]), float(sm[2])
-    else:
-        all_ops = float(ops_per_step)
+    (total_s, e2e_s), (all_ops,) = aggregate([total_s, e2e_s], [float(ops_per_step)], dev, world)
     if rank != 0:
         return 0
 
