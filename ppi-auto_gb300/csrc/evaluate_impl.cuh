@@ -117,6 +117,8 @@ __device__ __forceinline__ void store_row(float* p, int P, const float (&x)[R]) 
 // Measured on the polynomial workload: +44% in fast math.  The native
 // intrinsics and the double-precision parity routines stay unrolled (rolling
 // measured slightly slower there).
+// Records per iteration of a rolled case (copies of the routine inlined).
+constexpr int kRollWidth = 1;
 template <int OP, int MATH>
 __device__ constexpr bool roll_unary() {
    return MATH == kMathFast &&
@@ -280,6 +282,38 @@ __device__ __forceinline__ void local_tree(float* pe, int L, int reduce_max, int
    }
 }
 
+template <int EF, int R>
+__device__ __forceinline__ void error_row(const float (&v)[R], const float (&y)[R], float (&e)[R],
+                                          const float* cost, int cn) {
+#pragma unroll
+   for (int r = 0; r < R; ++r) e[r] = apply_error_t<EF>(v[r], y[r], cost, cn);
+}
+
+// Lane == tile position: each of this thread's R lanes adds its record's
+// error in record order, and stops at the first non-finite error
+// (accelerator.cl:236).  A tile wholly inside the dataset, on lanes none of
+// which has stopped, skips the per-record bounds test.
+template <int RM, int R>
+__device__ __forceinline__ void accumulate_lanes(float (&lacc)[R], uint32_t& ldone, const float (&e)[R],
+                                                 int base, int tid, int P, int T, int nlin, float fnlin) {
+   if (ldone == 0u && base + T <= nlin) {
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+         if (nonfinite(e[r])) { lacc[r] = FLT_MAX; ldone |= 1u << r; }
+         else lacc[r] = reduce1(RM, lacc[r], e[r], fnlin);
+      }
+      return;
+   }
+#pragma unroll
+   for (int r = 0; r < R; ++r) {
+      const int n = base + tile_pos(tid, r, P);
+      if (n < nlin && !((ldone >> r) & 1u)) {
+         if (nonfinite(e[r])) { lacc[r] = FLT_MAX; ldone |= 1u << r; }
+         else lacc[r] = reduce1(RM, lacc[r], e[r], fnlin);
+      }
+   }
+}
+
 // Everything the evaluation of one program needs (one population's dataset
 // and error settings, the program's translation).
 struct Job {
@@ -361,17 +395,15 @@ __device__ float evaluate_program(const Job& j, uint2* s_code, float* s_tile, in
       float ycol[R];
       load_row(s_tile + (size_t)trow * T + tid * 4, P, ycol);
       float e[R];
-#pragma unroll
-      for (int r = 0; r < R; ++r) e[r] = apply_error(j.ef, v[r], ycol[r], j.cost, j.cost_n);
+      switch (j.ef) {   // one switch per tile, not per record
+      case PPI_EF_ABS: error_row<PPI_EF_ABS>(v, ycol, e, j.cost, j.cost_n); break;
+      case PPI_EF_SQUARED: error_row<PPI_EF_SQUARED>(v, ycol, e, j.cost, j.cost_n); break;
+      case PPI_EF_MISCLASS: error_row<PPI_EF_MISCLASS>(v, ycol, e, j.cost, j.cost_n); break;
+      default: error_row<PPI_EF_COST>(v, ycol, e, j.cost, j.cost_n); break;
+      }
       if (aligned) {
-#pragma unroll
-         for (int r = 0; r < R; ++r) {
-            const int n = base + tile_pos(tid, r, P);
-            if (n < j.nlin && !((ldone >> r) & 1u)) {
-               if (nonfinite(e[r])) { lacc[r] = FLT_MAX; ldone |= 1u << r; }
-               else lacc[r] = reduce1(j.reduce_max, lacc[r], e[r], fnlin);
-            }
-         }
+         if (j.reduce_max) accumulate_lanes<1>(lacc, ldone, e, base, tid, P, T, j.nlin, fnlin);
+         else accumulate_lanes<0>(lacc, ldone, e, base, tid, P, T, j.nlin, fnlin);
       } else {
          __syncthreads();   // every thread is done with the rows: row 0 takes the errors
 #pragma unroll

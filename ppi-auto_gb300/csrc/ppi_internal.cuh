@@ -270,6 +270,15 @@ __device__ __forceinline__ float apply_error(int ef, float x, float y, const flo
 
 __device__ __forceinline__ bool nonfinite(float v) { return isinf(v) || isnan(v); }
 
+// apply_error with the error function fixed at compile time.
+template <int EF>
+__device__ __forceinline__ float apply_error_t(float x, float y, const float* cost, int cn) {
+   if constexpr (EF == PPI_EF_ABS) return fabsf(x - y);
+   else if constexpr (EF == PPI_EF_SQUARED) { const float d = x - y; return d * d; }
+   else if constexpr (EF == PPI_EF_MISCLASS) return (x != y) ? 1.0f : 0.0f;
+   else return apply_error(PPI_EF_COST, x, y, cost, cn);
+}
+
 // ---------------------------------------------------------------------------
 // One population of a batch (device memory).
 struct PopDesc {
