@@ -523,6 +523,8 @@ ppi_status ppi_batch_evaluate(ppi_batch* b, const int32_t* ph, const float* eph,
    std::memcpy(fitness, b->h_fit, T * 4);
    if (best_index) std::memcpy(best_index, b->h_best, (size_t)b->n_pops * 4);
    cudaEventElapsedTime(&b->last_ms, b->ev0, b->ev1);
+   if (*b->h_status & kStatusStageTimeout)
+      return bfail(b, PPI_ERR_DEVICE_STATUS, "a tile copy did not complete (bounded wait expired)");
    if (*b->h_status & kStatusUnsupportedProgram)
       return bfail(b, PPI_ERR_UNSUPPORTED, "a malformed program needs a deeper stack than supported");
    return PPI_OK;

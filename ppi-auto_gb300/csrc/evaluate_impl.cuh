@@ -223,12 +223,37 @@ __device__ __noinline__ void run_generic(const uint2* __restrict__ code, const f
    }
 }
 
+// ---- tile staging: TMA bulk copies completed on an mbarrier ----------------
+// Iterations of the barrier wait before giving up (the copies are from valid
+// global memory into this CTA's shared memory, so the limit is a safety net:
+// reaching it records kStatusStageTimeout and the tile is used as it is).
+constexpr int kStageWaitLimit = 1 << 24;
+
+struct Stager {
+   uint64_t* bar;      // shared-memory mbarrier (arrival count 1)
+   uint32_t phase;     // parity of the phase the next tile completes
+};
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+// One thread, once per CTA, before the first tile; then __syncthreads.
+__device__ __forceinline__ void stager_init(uint64_t* bar) {
+   asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(bar)));
+   asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
 // Stage the records [base, base + T) of the program's staged columns (tile
 // rows s .. s+k-1, from the code header) and of the target column (row s+k),
 // and prefetch into L2 the same records of the columns it reads directly.
+// When the tile starts on a 16-byte boundary (always, except DP over a lane
+// count that is not a multiple of 4) one thread copies each column's segment
+// with cp.async.bulk (TMA) and every thread waits on the mbarrier; otherwise
+// the threads copy with 16-byte loads.  All threads call it.
 __device__ __forceinline__ void stage_tile(const float* data, int ncol, int ld, const uint2* s_code,
-                                           float* s_tile, int base, int T, int tid, int P) {
-   const bool vec = (base & 3) == 0;
+                                           float* s_tile, int base, int T, int tid, int P, Stager& st,
+                                           int* status) {
    const uint2 hdr = s_code[0];
    const int k = (int)hdr.x, s = (int)(hdr.y & 0xFFFFu), d = (int)(hdr.y >> 16);
    const int lines = T / 32;   // 128-byte lines of one column's tile segment
@@ -241,18 +266,49 @@ __device__ __forceinline__ void stage_tile(const float* data, int ncol, int ld, 
          asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
       }
    }
+   const bool bulk = (base & 3) == 0 && (reinterpret_cast<uintptr_t>(data) & 15) == 0 && (ld & 3) == 0;
+   if (bulk) {
+      // floats per column segment: the tile, or what is left of the column
+      const int nf = min(T, ld - base);
+      const uint32_t bytes = (uint32_t)nf * 4u;
+      if (tid == 0) {
+         // earlier generic-proxy writes to these rows before the async copies
+         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+         asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(st.bar)),
+                      "r"(bytes * (uint32_t)(k + 1))
+                      : "memory");
+         for (int j = 0; j <= k; ++j) {
+            const uint2 pair = s_code[1 + (j >> 1)];
+            const int cidx = (j == k) ? ncol - 1 : (int)((j & 1) ? pair.y : pair.x);
+            const float* src = data + (size_t)cidx * ld + base;
+            float* dst = s_tile + (size_t)(s + j) * T;
+            asm volatile(
+                "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                    smem_addr(dst)),
+                "l"(src), "r"(bytes), "r"(smem_addr(st.bar))
+                : "memory");
+         }
+      }
+      uint32_t done = 0;
+      for (int it = 0; it < kStageWaitLimit && !done; ++it) {
+         asm volatile(
+             "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+             : "=r"(done)
+             : "r"(smem_addr(st.bar)), "r"(st.phase)
+             : "memory");
+      }
+      if (!done && tid == 0) atomicOr(status, kStatusStageTimeout);
+      st.phase ^= 1u;
+      return;
+   }
    for (int j = 0; j <= k; ++j) {
       const uint2 pair = s_code[1 + (j >> 1)];
       const int cidx = (j == k) ? ncol - 1 : (int)((j & 1) ? pair.y : pair.x);
       const float* src = data + (size_t)cidx * ld + base;
       float* dst = s_tile + (size_t)(s + j) * T;
       for (int t = tid * 4; t < T; t += P * 4) {
-         if (vec && base + t + 3 < ld) {
-            *reinterpret_cast<float4*>(dst + t) = __ldg(reinterpret_cast<const float4*>(src + t));
-         } else {
 #pragma unroll
-            for (int j = 0; j < 4; ++j) dst[t + j] = (base + t + j < ld) ? __ldg(src + t + j) : 0.0f;
-         }
+         for (int q = 0; q < 4; ++q) dst[t + q] = (base + t + q < ld) ? __ldg(src + t + q) : 0.0f;
       }
    }
 }
@@ -337,7 +393,7 @@ struct Job {
 // accumulators and lanes bytes of lane-finished flags.
 template <int MATH, int R, int OPSET, int D>
 __device__ float evaluate_program(const Job& j, uint2* s_code, float* s_tile, int* status, int tid,
-                                  int P) {
+                                  int P, Stager& st) {
    const int T = P * R;
    const int L = j.lanes;
    const bool aligned = j.strategy == PPI_STRATEGY_PDP && L == T;
@@ -380,7 +436,7 @@ __device__ float evaluate_program(const Job& j, uint2* s_code, float* s_tile, in
    bool ddone = false;
    for (int base = 0; base < j.nlin; base += Teff) {
       __syncthreads();
-      stage_tile(j.data, j.ncol, j.ld, s_code, s_tile, base, T, tid, P);
+      stage_tile(j.data, j.ncol, j.ld, s_code, s_tile, base, T, tid, P, st, status);
       __syncthreads();
       float v[R];
       if (kind != kKindGeneric) {
@@ -479,6 +535,10 @@ template <int MATH, int R, int OPSET, int D>
 __global__ void __launch_bounds__(128, 4) eval_kernel(const EvalArgs a) {
    extern __shared__ __align__(16) unsigned char smem_raw[];
    __shared__ int s_prog;
+   __shared__ __align__(8) uint64_t s_bar;
+   if (threadIdx.x == 0) stager_init(&s_bar);
+   __syncthreads();
+   Stager st{&s_bar, 0u};
    const int P = blockDim.x, tid = threadIdx.x;
    uint2* s_code = reinterpret_cast<uint2*>(smem_raw);
    float* s_tile = reinterpret_cast<float*>(smem_raw + code_bytes(a.code_stride));
@@ -502,7 +562,7 @@ __global__ void __launch_bounds__(128, 4) eval_kernel(const EvalArgs a) {
       }
       j.size = a.size[prog];
       j.code = a.code + (size_t)prog * a.code_stride;
-      const float fit = evaluate_program<MATH, R, OPSET, D>(j, s_code, s_tile, a.status, tid, P);
+      const float fit = evaluate_program<MATH, R, OPSET, D>(j, s_code, s_tile, a.status, tid, P, st);
       if (tid == 0) {
          a.fitness[prog] = fit;
          atomicMin(a.best_key, fitness_key(fit, prog));
@@ -527,6 +587,10 @@ template <int MATH, int R, int OPSET, int D>
 __global__ void __launch_bounds__(128, 4) eval_batch_kernel(const BatchArgs a) {
    extern __shared__ __align__(16) unsigned char smem_raw[];
    __shared__ int s_item;
+   __shared__ __align__(8) uint64_t s_bar;
+   if (threadIdx.x == 0) stager_init(&s_bar);
+   __syncthreads();
+   Stager st{&s_bar, 0u};
    const int P = blockDim.x, tid = threadIdx.x;
    uint2* s_code = reinterpret_cast<uint2*>(smem_raw);
    float* s_tile = reinterpret_cast<float*>(smem_raw + code_bytes(a.code_stride));
@@ -549,7 +613,7 @@ __global__ void __launch_bounds__(128, 4) eval_batch_kernel(const BatchArgs a) {
       j.size = a.size[g];
       j.code = a.code + (size_t)g * a.code_stride;
       j.rows_cap = a.rows;
-      const float fit = evaluate_program<MATH, R, OPSET, D>(j, s_code, s_tile, a.status, tid, P);
+      const float fit = evaluate_program<MATH, R, OPSET, D>(j, s_code, s_tile, a.status, tid, P, st);
       if (tid == 0) {
          const int local = g - pd.prog_begin;
          a.fitness[g] = fit;
@@ -568,6 +632,11 @@ __global__ void __launch_bounds__(128, 4) eval_batch_kernel(const BatchArgs a) {
 template <int MATH, int R, int OPSET>
 __global__ void __launch_bounds__(128, 4) predict_kernel(const PredictArgs a) {
    extern __shared__ __align__(16) unsigned char smem_raw[];
+   __shared__ __align__(8) uint64_t s_bar;
+   __shared__ int s_status_unused;
+   if (threadIdx.x == 0) stager_init(&s_bar);
+   __syncthreads();
+   Stager st{&s_bar, 0u};
    const int P = blockDim.x, tid = threadIdx.x, T = P * R;
    const int2 m = a.meta[0];
    uint2* s_code = reinterpret_cast<uint2*>(smem_raw);
@@ -580,7 +649,7 @@ __global__ void __launch_bounds__(128, 4) predict_kernel(const PredictArgs a) {
    for (int base = blockIdx.x * T; base < a.nlin; base += gridDim.x * T) {
       __syncthreads();
       if (runs)
-         stage_tile(a.data, a.ncol, a.ld, s_code, s_tile, base, T, tid, P);
+         stage_tile(a.data, a.ncol, a.ld, s_code, s_tile, base, T, tid, P, st, &s_status_unused);
       __syncthreads();
       float v[R];
       if (kind == kKindFast || kind == kKindWide) {

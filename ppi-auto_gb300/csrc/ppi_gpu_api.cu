@@ -329,6 +329,8 @@ ppi_status ppi_gpu_evaluate_wait(ppi_gpu* h) {
    std::memcpy(h->out_fit, h->h_fit, (size_t)h->pending_n * sizeof(float));
    if (h->out_best) *h->out_best = *h->h_best;
    cudaEventElapsedTime(&h->last_ms, h->ev0, h->ev1);
+   if (*h->h_status & kStatusStageTimeout)
+      return fail(h, PPI_ERR_DEVICE_STATUS, "a tile copy did not complete (bounded wait expired)");
    if (*h->h_status & kStatusUnsupportedProgram)
       return fail(h, PPI_ERR_UNSUPPORTED,
                   "a malformed program needs a deeper stack than the generic interpreter's");
@@ -615,6 +617,8 @@ ppi_status ppi_gpu_decode_evaluate(ppi_gpu* h, const uint8_t* genomes, int32_t n
    std::memcpy(fitness, h->h_fit, (size_t)n * sizeof(float));
    if (best_index) *best_index = *h->h_best;
    cudaEventElapsedTime(&h->last_ms, h->ev0, h->ev1);
+   if (*h->h_status & kStatusStageTimeout)
+      return fail(h, PPI_ERR_DEVICE_STATUS, "a tile copy did not complete (bounded wait expired)");
    if (*h->h_status & kStatusUnsupportedProgram)
       return fail(h, PPI_ERR_UNSUPPORTED, "a program needs a deeper stack than supported");
    return PPI_OK;

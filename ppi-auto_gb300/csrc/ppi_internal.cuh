@@ -64,7 +64,7 @@ struct DevStats {
 };
 
 // Status bits reported by the kernels.
-enum : int { kStatusUnsupportedProgram = 1 };
+enum : int { kStatusUnsupportedProgram = 1, kStatusStageTimeout = 2 };
 
 // Accumulator-machine instructions.  Each is a uint2: .x = instruction id
 // below, .y = immediate: float bits of a constant, or a row index.
