@@ -531,8 +531,13 @@ __device__ float evaluate_program(const Job& j, uint2* s_code, float* s_tile, in
 
 // One population: a persistent grid pulls program indices from a device
 // counter; the last CTA to finish turns the packed arg-min into the index.
+// Resident CTAs per SM the register allocation is bounded for: the fast and
+// native interpreters fit 80 registers a thread (6 CTAs of 128 threads), the
+// parity one needs the double-precision transcendentals' registers (4 CTAs).
+constexpr int min_ctas_per_sm(int math) { return math == kMathParity ? 4 : 6; }
+
 template <int MATH, int R, int OPSET, int D>
-__global__ void __launch_bounds__(128, 4) eval_kernel(const EvalArgs a) {
+__global__ void __launch_bounds__(128, min_ctas_per_sm(MATH)) eval_kernel(const EvalArgs a) {
    extern __shared__ __align__(16) unsigned char smem_raw[];
    __shared__ int s_prog;
    __shared__ __align__(8) uint64_t s_bar;
@@ -584,7 +589,7 @@ __global__ void __launch_bounds__(128, 4) eval_kernel(const EvalArgs a) {
 // own arg-min key and completion counter, and the CTA that finishes a
 // population's last program writes that population's best index.
 template <int MATH, int R, int OPSET, int D>
-__global__ void __launch_bounds__(128, 4) eval_batch_kernel(const BatchArgs a) {
+__global__ void __launch_bounds__(128, min_ctas_per_sm(MATH)) eval_batch_kernel(const BatchArgs a) {
    extern __shared__ __align__(16) unsigned char smem_raw[];
    __shared__ int s_item;
    __shared__ __align__(8) uint64_t s_bar;
