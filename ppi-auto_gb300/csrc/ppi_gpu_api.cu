@@ -68,12 +68,15 @@ struct ppi_gpu {
    float last_ms = 0.0f;
    int last_launches = 0;
    // constant adjoint (allocated on first use)
-   uint4* d_adj_code = nullptr;
+   uint2* d_adj_code = nullptr;
    int2* d_adj_meta = nullptr;
    float* d_grad = nullptr;
-   int* d_adj_stats = nullptr;   // max rows, max constants, work queues of the two passes
+   int* d_adj_stats = nullptr;   // max rows, max constants, work queues of the occupancy levels
    int* h_adj_stats = nullptr;
    int* d_adj_order = nullptr;
+   double* d_adj_psum = nullptr;   // per program and chunk: the constants' sums
+   int* d_adj_pbad = nullptr;
+   size_t adj_chunk_cap = 0;       // program x chunk entries allocated
    std::vector<int2> h_adj_meta;
    std::vector<int> h_adj_order;
 };
@@ -109,7 +112,7 @@ void free_all(ppi_gpu* h) {
    free_decode_tables(&h->dec);
    cudaFreeHost(h->h_fit); cudaFreeHost(h->h_best); cudaFreeHost(h->h_status);
    cudaFree(h->d_adj_code); cudaFree(h->d_adj_meta); cudaFree(h->d_grad); cudaFree(h->d_adj_stats);
-   cudaFree(h->d_adj_order);
+   cudaFree(h->d_adj_order); cudaFree(h->d_adj_psum); cudaFree(h->d_adj_pbad);
    cudaFreeHost(h->h_adj_stats);
    if (h->ev0) cudaEventDestroy(h->ev0);
    if (h->ev1) cudaEventDestroy(h->ev1);
@@ -402,6 +405,14 @@ ppi_status ppi_gpu_predict(ppi_gpu* h, const int32_t* ph, const float* eph, int3
    return PPI_OK;
 }
 
+// Adjoint launch planning: occupancy levels per R (CTAs per SM, 0 = the
+// narrow fallback), the smallest level at which R = 8 is kept, and the stats
+// block (max rows, constants, code words; a work queue per launch group).
+constexpr int kAdjLevels = 16;
+constexpr int kAdjR8MinCtas = 1;
+constexpr int kAdjMaxChunks = 16;   // record chunks (work items) per program
+constexpr int kAdjStats = 3 + 2 * kAdjLevels;
+
 ppi_status ppi_gpu_constant_gradient(ppi_gpu* h, const int32_t* ph, const float* eph,
                                      const int32_t* size, int32_t n, float* gradient) {
    ppi_status s = check_ready(h, n);
@@ -417,79 +428,131 @@ ppi_status ppi_gpu_constant_gradient(ppi_gpu* h, const int32_t* ph, const float*
       PPI_CUDA(h, dalloc(&h->d_adj_code, pop * stride));
       PPI_CUDA(h, dalloc(&h->d_adj_meta, pop));
       PPI_CUDA(h, dalloc(&h->d_grad, pop * ms));
-      PPI_CUDA(h, dalloc(&h->d_adj_stats, 4));
-      PPI_CUDA(h, cudaMallocHost(reinterpret_cast<void**>(&h->h_adj_stats), 4 * sizeof(int)));
+      PPI_CUDA(h, dalloc(&h->d_adj_stats, kAdjStats));
+      PPI_CUDA(h, cudaMallocHost(reinterpret_cast<void**>(&h->h_adj_stats), kAdjStats * sizeof(int)));
    }
    cudaStream_t st = h->stream;
    PPI_CUDA(h, cudaMemcpyAsync(h->d_ph, ph, (size_t)n * ms * 4, cudaMemcpyHostToDevice, st));
    PPI_CUDA(h, cudaMemcpyAsync(h->d_eph, eph, (size_t)n * ms * 4, cudaMemcpyHostToDevice, st));
    PPI_CUDA(h, cudaMemcpyAsync(h->d_size, size, (size_t)n * 4, cudaMemcpyHostToDevice, st));
-   PPI_CUDA(h, cudaMemsetAsync(h->d_adj_stats, 0, 4 * sizeof(int), st));
+   PPI_CUDA(h, cudaMemsetAsync(h->d_adj_stats, 0, kAdjStats * sizeof(int), st));
+   PPI_CUDA(h, cudaMemsetAsync(h->d_status, 0, sizeof(int), st));
    AdjointTranslateArgs t{};
    t.phenotype = h->d_ph; t.ephemeral = h->d_eph; t.size = h->d_size; t.n = n;
    t.max_size = h->cfg.max_size; t.ncol = h->ncol;
    t.lut = h->d_lut; t.lut_min = h->lut_min; t.lut_len = h->lut_len;
    t.code = h->d_adj_code; t.code_stride = stride; t.meta = h->d_adj_meta; t.work = h->d_work;
-   t.max_rows = h->d_adj_stats; t.max_consts = h->d_adj_stats + 1;
+   t.max_rows = h->d_adj_stats; t.max_consts = h->d_adj_stats + 1; t.max_code = h->d_adj_stats + 2;
    PPI_CUDA(h, launch_adjoint_translate(t, st));
    h->h_adj_meta.resize((size_t)n);
-   PPI_CUDA(h, cudaMemcpyAsync(h->h_adj_stats, h->d_adj_stats, 2 * sizeof(int), cudaMemcpyDeviceToHost, st));
+   PPI_CUDA(h, cudaMemcpyAsync(h->h_adj_stats, h->d_adj_stats, 3 * sizeof(int), cudaMemcpyDeviceToHost, st));
    PPI_CUDA(h, cudaMemcpyAsync(h->h_adj_meta.data(), h->d_adj_meta, (size_t)n * sizeof(int2),
                                cudaMemcpyDeviceToHost, st));
    PPI_CUDA(h, cudaStreamSynchronize(st));
-   // Two passes over 128-thread CTAs (4 records each): the programs whose
-   // tape fits the tile at the kernel's best occupancy, then the rest with a
-   // tile for the longest tape (a narrower CTA when 128 threads do not fit).
+   // Launch groups (R, L): a program runs at R = 8 records per thread when
+   // that tile holds its rows (slots, kept values, columns, target) at
+   // kAdjR8MinCtas or more resident CTAs per SM, else at R = 4; within an R,
+   // at the occupancy level L (CTAs per SM) with the most CTAs whose tile
+   // holds it.  One persistent launch per group that has programs, longest
+   // programs first.  Programs too wide for a 128-thread CTA at one per SM
+   // run last on narrower CTAs (level 0).
    const int rows_max = std::max(1, h->h_adj_stats[0]), nconst = std::max(1, h->h_adj_stats[1]);
-   auto occ = [&](int P, int rows) {
+   const int words = std::max(1, h->h_adj_stats[2]);
+   auto occ = [&](int R, int P, int rows) {
       int per_sm = 0;
-      const size_t smem = adjoint_smem_bytes(stride, nconst, rows, P);
-      if (smem > 200 * 1024 || adjoint_occupancy(h->cfg.math, h->opset, P, smem, &per_sm) != cudaSuccess)
+      const size_t smem = adjoint_smem_bytes(words, nconst, rows, P, R);
+      if (smem > 200 * 1024 || adjoint_occupancy(h->cfg.math, h->opset, R, P, smem, &per_sm) != cudaSuccess)
          return 0;
       return per_sm;
    };
    const int P1 = 128;
-   const int top = occ(P1, 1);
-   if (top < 1) return fail(h, PPI_ERR_UNSUPPORTED, "adjoint kernel does not fit on an SM");
-   int rows1 = 1;
-   while (rows1 < rows_max && occ(P1, rows1 + 1) >= top) ++rows1;
-   int P2 = 128;
-   while (P2 > 32 && occ(P2, rows_max) < 1) P2 /= 2;
-   if (occ(P2, rows_max) < 1) return fail(h, PPI_ERR_UNSUPPORTED, "program tape too long for shared memory");
-   h->h_adj_order.clear();
-   for (int i = 0; i < n; ++i)
-      if ((h->h_adj_meta[i].x >> 8) <= rows1) h->h_adj_order.push_back(i);
-   const int n1 = (int)h->h_adj_order.size();
-   for (int i = 0; i < n; ++i)
-      if ((h->h_adj_meta[i].x >> 8) > rows1) h->h_adj_order.push_back(i);
+   struct Levels {
+      int R, top, rows[kAdjLevels];
+   } lv[2] = {{8, 0, {0}}, {4, 0, {0}}};
+   for (Levels& v : lv) {
+      v.top = std::min(occ(v.R, P1, 1), kAdjLevels - 1);
+      for (int L = v.top, r = 1; L >= 1; --L) {
+         while (r < rows_max && occ(v.R, P1, r + 1) >= L) ++r;
+         v.rows[L] = occ(v.R, P1, r) >= L ? r : 0;
+      }
+   }
+   if (lv[1].top < 1) return fail(h, PPI_ERR_UNSUPPORTED, "adjoint kernel does not fit on an SM");
+   int P0 = 128;
+   while (P0 > 32 && occ(4, P0, rows_max) < 1) P0 /= 2;
+   if (occ(4, P0, rows_max) < 1) return fail(h, PPI_ERR_UNSUPPORTED, "program too wide for shared memory");
+   auto level_of = [&](const Levels& v, int rows) {
+      for (int L = v.top; L >= 1; --L)
+         if (rows <= v.rows[L]) return L;
+      return 0;
+   };
+   // group index: R = 8 groups 0 .. kAdjLevels-1, R = 4 groups kAdjLevels ..
+   auto group_of = [&](int rows) {
+      const int L8 = level_of(lv[0], rows);
+      if (L8 >= kAdjR8MinCtas) return L8;
+      return kAdjLevels + level_of(lv[1], rows);
+   };
+   const int ngroups = 2 * kAdjLevels;
+   h->h_adj_order.resize((size_t)n);
+   std::vector<int> count(ngroups, 0), start(ngroups, 0), fill(ngroups, 0);
+   for (int i = 0; i < n; ++i) ++count[group_of(h->h_adj_meta[i].x >> 8)];
+   for (int gi = 0, o = 0; gi < ngroups; ++gi) { start[gi] = o; fill[gi] = o; o += count[gi]; }
+   for (int i = 0; i < n; ++i) h->h_adj_order[fill[group_of(h->h_adj_meta[i].x >> 8)]++] = i;
+   for (int gi = 0; gi < ngroups; ++gi)
+      std::stable_sort(h->h_adj_order.begin() + start[gi], h->h_adj_order.begin() + start[gi] + count[gi],
+                       [&](int x, int y) { return size[x] > size[y]; });
+   // chunks of each program's records (work items): about 8 tiles or more
+   // each, at most kAdjMaxChunks per program
+   const int n_chunks = std::max(1, std::min(kAdjMaxChunks, (h->nlin + 8191) / 8192));
+   const int chunk = ((h->nlin + n_chunks - 1) / n_chunks + 1023) / 1024 * 1024;
+   const int chunks = (h->nlin + chunk - 1) / chunk;
+   const size_t entries = (size_t)n * chunks;
+   if (entries > h->adj_chunk_cap) {
+      cudaFree(h->d_adj_psum);
+      cudaFree(h->d_adj_pbad);
+      h->d_adj_psum = nullptr;
+      h->d_adj_pbad = nullptr;
+      h->adj_chunk_cap = 0;
+      PPI_CUDA(h, dalloc(&h->d_adj_psum, entries * kAdjMaxConsts));
+      PPI_CUDA(h, dalloc(&h->d_adj_pbad, entries));
+      h->adj_chunk_cap = entries;
+   }
    if (!h->d_adj_order) PPI_CUDA(h, dalloc(&h->d_adj_order, pop));
    PPI_CUDA(h, cudaMemcpyAsync(h->d_adj_order, h->h_adj_order.data(), (size_t)n * sizeof(int),
                                cudaMemcpyHostToDevice, st));
    AdjointArgs a{};
    a.data = h->d_data; a.nlin = h->nlin; a.ncol = h->ncol; a.ld = h->ld;
-   a.code = h->d_adj_code; a.code_stride = stride; a.meta = h->d_adj_meta;
+   a.code = h->d_adj_code; a.code_stride = stride; a.code_words = words; a.meta = h->d_adj_meta;
    a.max_size = h->cfg.max_size; a.ef = h->cfg.error_fn; a.prot = h->cfg.protected_fns ? 1 : 0;
-   a.max_consts = nconst; a.grad = h->d_grad;
+   a.max_consts = nconst; a.status = h->d_status;
+   a.chunk = chunk; a.n_chunks = chunks; a.psum = h->d_adj_psum; a.pbad = h->d_adj_pbad;
    PPI_CUDA(h, cudaEventRecord(h->ev0, st));
    h->last_launches = 1;
-   if (n1 > 0) {
-      a.order = h->d_adj_order; a.n_items = n1; a.queue = reinterpret_cast<unsigned*>(h->d_adj_stats + 2);
-      PPI_CUDA(h, launch_adjoint(h->cfg.math, h->opset, a, P1, std::max(1, std::min(n1, top * h->sm_count)),
-                                 adjoint_smem_bytes(stride, nconst, rows1, P1), st));
+   for (int gi = 0; gi < ngroups; ++gi) {
+      if (count[gi] == 0) continue;
+      const Levels& v = lv[gi < kAdjLevels ? 0 : 1];
+      const int L = gi % kAdjLevels;
+      const int P = L > 0 ? P1 : P0, rows = L > 0 ? v.rows[L] : rows_max;
+      const int per = L > 0 ? L : occ(v.R, P0, rows_max);
+      a.order = h->d_adj_order + start[gi]; a.n_items = count[gi] * chunks;
+      a.queue = reinterpret_cast<unsigned*>(h->d_adj_stats + 3 + gi);
+      PPI_CUDA(h, launch_adjoint(h->cfg.math, h->opset, v.R, a, P,
+                                 std::max(1, std::min(a.n_items, per * h->sm_count)),
+                                 adjoint_smem_bytes(words, nconst, rows, P, v.R), st));
       ++h->last_launches;
    }
-   if (n1 < n) {
-      const int per2 = occ(P2, rows_max);
-      a.order = h->d_adj_order + n1; a.n_items = n - n1;
-      a.queue = reinterpret_cast<unsigned*>(h->d_adj_stats + 3);
-      PPI_CUDA(h, launch_adjoint(h->cfg.math, h->opset, a, P2, std::max(1, std::min(n - n1, per2 * h->sm_count)),
-                                 adjoint_smem_bytes(stride, nconst, rows_max, P2), st));
-      ++h->last_launches;
-   }
+   AdjointFinishArgs fa{};
+   fa.code = h->d_adj_code; fa.code_stride = stride; fa.meta = h->d_adj_meta; fa.n = n;
+   fa.max_size = h->cfg.max_size; fa.max_consts = nconst; fa.n_chunks = chunks;
+   fa.psum = h->d_adj_psum; fa.pbad = h->d_adj_pbad; fa.grad = h->d_grad;
+   PPI_CUDA(h, launch_adjoint_finish(fa, st));
+   ++h->last_launches;
    PPI_CUDA(h, cudaEventRecord(h->ev1, st));
    PPI_CUDA(h, cudaMemcpyAsync(gradient, h->d_grad, (size_t)n * ms * 4, cudaMemcpyDeviceToHost, st));
+   PPI_CUDA(h, cudaMemcpyAsync(h->h_status, h->d_status, sizeof(int), cudaMemcpyDeviceToHost, st));
    PPI_CUDA(h, cudaStreamSynchronize(st));
    cudaEventElapsedTime(&h->last_ms, h->ev0, h->ev1);
+   if (*h->h_status & kStatusStageTimeout)
+      return fail(h, PPI_ERR_DEVICE_STATUS, "a tile copy did not complete (bounded wait expired)");
    return PPI_OK;
 }
 

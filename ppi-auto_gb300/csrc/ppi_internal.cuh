@@ -375,9 +375,11 @@ struct PredictArgs {
 enum : int { kAdjInvalid = 0, kAdjValid = 1, kAdjUnsupported = 2 };
 // Most ephemeral constants of one program the adjoint differentiates.
 constexpr int kAdjMaxConsts = 32;
-// uint4 entries of one program's tape code: header, two per operator, one
-// per constant or literal.
-inline int adjoint_code_stride(int max_size) { return 1 + 3 * max_size; }
+// uint2 words of one program's adjoint code: the column header and list,
+// the forward bytecode (an instruction per token plus the value pushes),
+// the reverse instructions (two words each, at most two per operator) and
+// the operand table.
+inline int adjoint_code_stride(int max_size) { return 8 * max_size + 8; }
 
 struct AdjointTranslateArgs {
    const int32_t* phenotype;
@@ -386,32 +388,49 @@ struct AdjointTranslateArgs {
    int n, max_size, ncol;
    const int2* lut;
    int lut_min, lut_len;
-   uint4* code;                // program i at code + i * code_stride
+   uint2* code;                // program i at code + i * code_stride
    int code_stride;
    int2* meta;                 // {kAdj* | rows << 8, code length}
    uint2* work;                // n x 2 max_size scratch
    int* max_rows;              // over the population (atomicMax)
    int* max_consts;
+   int* max_code;              // longest code (uint2 words)
 };
 
 struct AdjointArgs {
    const float* data;          // column-major, column c at data + c * ld
    int nlin, ncol, ld;
-   const uint4* code;
+   const uint2* code;
    int code_stride;
+   int code_words;             // shared-memory code region: the longest program's code
    const int2* meta;
    int max_size, ef, prot, max_consts;
-   const int* order;           // programs of this pass (nullptr: 0 .. n_items-1)
-   int n_items;
-   float* grad;                // n x max_size
+   const int* order;           // programs of this launch
+   int n_items;                // work items: programs x n_chunks
+   int chunk, n_chunks;        // records per work item (a multiple of 1024), chunks per program
+   double* psum;               // [program][chunk][max_consts] sums of the chunks
+   int* pbad;                  // [program][chunk] a non-finite error was met
    unsigned* queue;
+   int* status;                // kStatus* bits (tile copy timeouts)
+};
+
+struct AdjointFinishArgs {
+   const uint2* code;
+   int code_stride;
+   const int2* meta;
+   int n, max_size, max_consts, n_chunks;
+   const double* psum;
+   const int* pbad;
+   float* grad;                // n x max_size
 };
 
 cudaError_t launch_adjoint_translate(const AdjointTranslateArgs& a, cudaStream_t s);
-cudaError_t launch_adjoint(int math, int opset, const AdjointArgs& a, int block, int grid, size_t smem,
+cudaError_t launch_adjoint_finish(const AdjointFinishArgs& a, cudaStream_t s);
+// R: records per thread, 4 or 8 (kernels of adjoint_r4.cu / adjoint_r8.cu).
+cudaError_t launch_adjoint(int math, int opset, int R, const AdjointArgs& a, int block, int grid, size_t smem,
                            cudaStream_t s);
-cudaError_t adjoint_occupancy(int math, int opset, int block, size_t smem, int* per_sm);
-size_t adjoint_smem_bytes(int code_stride, int max_consts, int rows, int block);
+cudaError_t adjoint_occupancy(int math, int opset, int R, int block, size_t smem, int* per_sm);
+size_t adjoint_smem_bytes(int code_words, int max_consts, int rows, int block, int R);
 
 // Evaluator launch geometry: lanes, block size P, records per thread R, and
 // for the main and the wide pass the row budget, dynamic shared memory and a
