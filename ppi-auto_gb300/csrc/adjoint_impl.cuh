@@ -139,13 +139,36 @@ __device__ __forceinline__ void adj_deliver(uint32_t kind, uint32_t dst, const f
    X(PPI_OP_LESSEQUAL) X(PPI_OP_EQUAL) X(PPI_OP_NOTEQUAL) X(PPI_OP_MEAN) X(PPI_OP_MAX) X(PPI_OP_MIN) \
    X(PPI_OP_MOD) X(PPI_OP_POW)
 
+// The sine and cosine cases' long routines (cosf, sinf of the operand) run
+// rolled: the R operands rotate through one inlined copy, which keeps the
+// reverse interpreter's code small (it shares the instruction cache with the
+// forward one).
+constexpr bool kAdjRollTrig = true;
+template <int OP, int R>
+__device__ __forceinline__ void adj_trig_case(const float (&g)[R], float (&x)[R], float (&d0)[R]) {
+#pragma unroll 1
+   for (int r = 0; r < R; ++r) {
+      const float t = OP == PPI_OP_SIN ? cosf(x[0]) : sinf(x[0]);
+#pragma unroll
+      for (int q = 0; q < R - 1; ++q) x[q] = x[q + 1];
+      x[R - 1] = t;
+   }
+#pragma unroll
+   for (int r = 0; r < R; ++r) d0[r] = OP == PPI_OP_SIN ? g[r] * x[r] : -(g[r] * x[r]);
+}
+
 #define ADJ_REV_CASE(OP)                                                                  \
    case OP:                                                                               \
       if constexpr (adj_reads_a(OP)) adj_operand(i0.y & 0xFFFFu, mine, T, P, tab, x);      \
       if constexpr (adj_reads_b(OP)) adj_operand(i0.y >> 16, mine, T, P, tab, y);          \
       if constexpr (adj_reads_v(OP)) load_row(mine + (size_t)(i0.x >> 16) * T, P, v);      \
-      _Pragma("unroll") for (int r = 0; r < R; ++r)                                       \
-         adj_bp<OP>(g[r], x[r], y[r], 0.0f, v[r], prot, d0[r], d1[r], d2[r]);             \
+      if constexpr (kAdjRollTrig && (OP == PPI_OP_SIN || OP == PPI_OP_COS)) {              \
+         adj_trig_case<OP, R>(g, x, d0);                                                   \
+         _Pragma("unroll") for (int r = 0; r < R; ++r) { d1[r] = 0.0f; d2[r] = 0.0f; }     \
+      } else {                                                                             \
+         _Pragma("unroll") for (int r = 0; r < R; ++r)                                    \
+            adj_bp<OP>(g[r], x[r], y[r], 0.0f, v[r], prot, d0[r], d1[r], d2[r]);          \
+      }                                                                                    \
       break;
 
 template <int OPSET, int R>

@@ -409,7 +409,7 @@ ppi_status ppi_gpu_predict(ppi_gpu* h, const int32_t* ph, const float* eph, int3
 // narrow fallback), the smallest level at which R = 8 is kept, and the stats
 // block (max rows, constants, code words; a work queue per launch group).
 constexpr int kAdjLevels = 16;
-constexpr int kAdjR8MinCtas = 1;
+constexpr int kAdjR8MinCtas = 4;
 constexpr int kAdjMaxChunks = 16;   // record chunks (work items) per program
 constexpr int kAdjStats = 3 + 2 * kAdjLevels;
 
