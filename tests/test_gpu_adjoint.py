@@ -176,3 +176,89 @@ def test_autograd_function_and_refinement(gpu_lib):
     fit_end, _ = ev.evaluate(ph, c.detach().numpy(), sz)
     end = np.median(fit_end[finite & (fit_end < FLT_MAX)])
     assert end < start
+
+
+@pytest.mark.parametrize("fixture", ["allops", "allops_prot"])
+def test_full_opcode_set_is_the_float_functions_gradient(gpu_lib, oracle_lib, fixture):
+    """Every opcode (comparisons, logic, IF_THEN_ELSE, MOD, POW, the
+    transcendentals, protected or not) through the full-set kernels, in
+    parity math: the gradient of the float function (oracle: float forward,
+    double reverse), piecewise-constant opcodes contributing 0."""
+    from helpers import ProgramGen, load_golden, make_evaluator, oracle_for
+    d = load_golden(fixture)
+    rng = np.random.default_rng(11 if fixture == "allops" else 12)
+    nfeat = d["rows"].shape[1] - 1
+    X = rng.normal(0, 2, (1500, nfeat)).astype(np.float32)
+    y = rng.normal(0, 2, 1500).astype(np.float32)
+    rows = np.concatenate([X, y[:, None]], 1)
+    gen = ProgramGen(d, rng, rows.shape[1])
+    progs = [gen.random(int(k)) for k in rng.integers(1, 16, 2000)]
+    ph, ep, sz = ProgramGen.rows(progs, 64)
+    # half of the leaves become constants (the generator draws leaf kinds
+    # evenly, and the fixtures name many literals)
+    from ppi_gpu import grammar as G
+    const = gen.by_op[G.OP["CONST"]][0]
+    leafsyms = set(s for op in gen.leaf for s in gen.by_op[op])
+    for i in range(len(sz)):
+        for k in range(sz[i]):
+            if ph[i, k] in leafsyms and rng.random() < 0.5:
+                ph[i, k], ep[i, k] = const, np.float32(rng.uniform(-3, 3))
+    ev = make_evaluator(d, "PDP", 0, "parity", population=len(sz), max_size=64, rows=rows)
+    grad = ev.constant_gradient(ph, ep, sz)
+    fit, _ = ev.evaluate(ph, ep, sz)
+    o = oracle_for(oracle_lib, d, rows=rows)
+    _, gff = o.adjoint64(ph, ep.astype(np.float64), sz, float_forward=True)
+    ok = _in_float_range(fit, gff)
+    rel = _rel(gff, grad, ok)
+    assert rel.size > 200   # most paths pass a piecewise-constant opcode (gradient 0)
+    assert (rel <= 1e-5).mean() >= 0.995, np.sort(rel)[-5:]
+    assert np.all(grad[fit == FLT_MAX] == 0.0)
+
+
+def test_record_chunks_and_wide_programs(gpu_lib, oracle_lib):
+    """20,000 records (several record chunks per program, the last one
+    partial) and programs up to 250 tokens over 64 columns: their rows
+    (columns, kept values) exceed what an 8-record tile holds at 4 CTAs per
+    SM, and the widest exceed a 128-thread CTA of 4 records, so every launch
+    group runs (8 and 4 records per thread, and the narrow-CTA fallback)."""
+    import ppi_gpu
+    from ppi_gpu import grammar as G
+    from ppi_gpu import workloads as W
+    from helpers import GRAMMARS
+    import os
+    rng = np.random.default_rng(21)
+    g = G.load(os.path.join(GRAMMARS, "config4_adjoint.bnf"))
+    nlin, nfeat = 20000, 64
+    X = rng.normal(0, 1, (nlin, nfeat)).astype(np.float32)
+    y = (X[:, 0] * X[:, 1] + np.sin(X[:, 2]) + rng.normal(0, 0.05, nlin)).astype(np.float32)
+    rows = np.concatenate([X, y[:, None]], 1)
+    lengths = np.concatenate([rng.integers(3, 40, 120), rng.integers(150, 251, 120)])
+    ph, ep = W.random_programs(rng, lengths, nfeat, g, p_unary=0.1, lo=-2.0, hi=2.0)
+    S = g.symbols
+    attr, const = S["T_ATTRIBUTE"], S["T_CONST"]
+    for i, k in enumerate(lengths):   # leaves: columns, and 1-8 constants
+        leaves = np.flatnonzero((ph[i, :k] == attr) | (ph[i, :k] == const))
+        ph[i, leaves] = attr
+        ep[i, leaves] = rng.integers(0, nfeat, len(leaves)).astype(np.float32)
+        pick = rng.choice(leaves, min(len(leaves), int(rng.integers(1, 9))), replace=False)
+        ph[i, pick] = const
+        ep[i, pick] = rng.uniform(-2.0, 2.0, len(pick)).astype(np.float32)
+    max_size = 256
+    phf = np.zeros((len(lengths), max_size), np.int32)
+    epf = np.zeros((len(lengths), max_size), np.float32)
+    phf[:, :ph.shape[1]] = ph
+    epf[:, :ep.shape[1]] = ep
+    sz = lengths.astype(np.int32)
+    ev = ppi_gpu.Evaluator(g.symbol_table_arrays(), max_size, len(sz), "PDP", 0, "squared", None, False,
+                           True, "parity")
+    ev.set_dataset(rows)
+    grad = ev.constant_gradient(phf, epf, sz)
+    assert ev.last_launch_count() >= 4   # at least two groups, plus translate and finish
+    fit, _ = ev.evaluate(phf, epf, sz)
+    o = oracle_lib.Oracle(rows, g.symbol_table_arrays(), "squared", None, False, True, False)
+    _, gff = o.adjoint64(phf, epf.astype(np.float64), sz, float_forward=True)
+    for part in (lengths < 40, lengths >= 150):
+        ok = _in_float_range(fit, gff) & part
+        rel = _rel(gff, grad, ok)
+        assert rel.size > 100
+        assert (rel <= 1e-5).mean() >= 0.995, np.sort(rel)[-5:]
