@@ -200,6 +200,20 @@ __global__ void adjoint_translate_kernel(const AdjointTranslateArgs a) {
 
    // ---- forward sweep: the evaluator's emission, plus the kept values -----
    {
+      // a push followed by a load of a tile row becomes one M_PUSH_LD
+      bool after_push = false;
+      uint32_t push_row = 0u;
+      auto emit = [&](uint32_t x, uint32_t y) {
+         if (after_push && x == M_LD_ROW && y < 0x10000u && push_row < 0x10000u) {
+            if (ncode - 1 < cap) code[ncode - 1] = make_uint2(M_PUSH_LD, push_row | (y << 16));
+            after_push = false;
+            return;
+         }
+         if (ncode < cap) code[ncode] = make_uint2(x, y);
+         ++ncode;
+         after_push = x == M_PUSH;
+         push_row = y;
+      };
       int fp = 0;
       frames[fp++] = aframe(0, 0, 0);
       auto finish = [&](int nd) {

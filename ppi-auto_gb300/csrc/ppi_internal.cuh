@@ -85,7 +85,9 @@ enum : uint32_t {
    M_BC_R = M_BC_L + 18,            //                        acc = op(imm, acc)
    M_ITE = M_BC_R + 18,             // + perm: rows a = imm & 0xFFFF, b = imm >> 16;
                                     //   roles of (acc, a, b) as (cond, then, else)
-   M_COUNT = M_ITE + 6
+   M_PUSH_LD = M_ITE + 6,           // row[imm & 0xFFFF] = acc; acc = row[imm >> 16]
+                                    //   (a push and the load after it, tile rows only)
+   M_COUNT = M_PUSH_LD + 1
 };
 static_assert(PPI_OP_TAN - PPI_OP_NOT + 1 == 25, "unary op count");
 static_assert(PPI_OP_DIV - PPI_OP_AND + 1 == 18, "binary op count");

@@ -239,9 +239,19 @@ __device__ int2 translate_program(const TranslateArgs& ta, int i, int sz) {
    if (fast) {
       int fp = 0;
       frames[fp++] = frame(0, 0, 0);
+      // a push followed by a load of a tile row becomes one M_PUSH_LD
+      bool after_push = false;
+      uint32_t push_row = 0u;
       auto emit = [&](uint32_t id, uint32_t imm) {
+         if (after_push && id == M_LD_ROW && imm < 0x10000u && push_row < 0x10000u) {
+            if (ncode - 1 < cap) code[ncode - 1] = make_uint2(M_PUSH_LD, push_row | (imm << 16));
+            after_push = false;
+            return;
+         }
          if (ncode < cap) code[ncode] = make_uint2(id, imm);
          ++ncode;
+         after_push = id == M_PUSH;
+         push_row = imm;
       };
       auto is_leaf = [&](int node) { return op_arity(node_op(w[node])) == 0; };
       auto leaf_attr = [&](int node) { return node_op(w[node]) == PPI_OP_ATTRIBUTE; };
