@@ -151,8 +151,21 @@ const char* plan_geometry(int strategy, int lanes, int math, int opset, int nlin
       while (rows < fit && occupancy(direct, rows + 1) >= top) ++rows;
       return rows;
    };
-   // main pass: programs whose columns all fit, lean kernel
-   const int rows = best_rows(0);
+   // main pass: programs whose columns all fit, lean kernel; when the whole
+   // population is resident in one wave at a larger tile, the larger tile
+   // (the most rows at which it still is: occupancy falls as rows grow)
+   int rows = best_rows(0);
+   if ((long long)occupancy(0, fit) * sm_count >= n_max) {
+      rows = fit;
+   } else if ((long long)occupancy(0, rows + 1) * sm_count >= n_max && rows < fit) {
+      int lo = rows + 1, hi = fit;   // occupancy(lo) fits, occupancy(hi) does not
+      while (hi - lo > 1) {
+         const int mid = (lo + hi) / 2;
+         if ((long long)occupancy(0, mid) * sm_count >= n_max) lo = mid;
+         else hi = mid;
+      }
+      rows = lo;
+   }
    // second pass: the rest, with the columns that do not fit read directly
    // (room at least for the deepest slot need and the target)
    const int rows2 = std::max(best_rows(1), std::min(fit, kSlots + 1));

@@ -209,8 +209,8 @@ def test_wide_dataset_staged_and_direct_columns(gpu_lib, oracle_lib, strat, lane
     the tile; programs reading 12-85 distinct columns stage the most-read
     ones and read the rest directly from global memory (with DP over 7 lanes
     the tiles start at records that are not multiples of 4, so those reads
-    are scalar).  The second evaluation runs with the row budget re-planned
-    from the first one's histogram; both must match the oracle bit for bit."""
+    are scalar).  Two evaluations in a row must both match the oracle bit
+    for bit."""
     d = load_golden("allops")
     rng = np.random.default_rng(77 + lanes)
     rows = _dataset(rng, 3000, 90)
@@ -221,7 +221,10 @@ def test_wide_dataset_staged_and_direct_columns(gpu_lib, oracle_lib, strat, lane
         progs.append([gen.op_tok(1)] + _sum_of_columns(gen, rng.integers(0, 90, k)))   # repeats
     rng.shuffle(progs)
     ph, ep, sz = ProgramGen.rows(progs, 200)
-    ev = make_evaluator(d, strat, lanes, "parity", population=len(sz), max_size=200, rows=rows)
+    # a population capacity far above one wave keeps the main tile at its
+    # occupancy-driven size (a population that fits one wave gets every row it
+    # can use), so the wide programs take the direct-read path
+    ev = make_evaluator(d, strat, lanes, "parity", population=20000, max_size=200, rows=rows)
     ref = oracle_for(oracle_lib, d, rows=rows).evaluate(ph, ep, sz, strat, ev.lanes, 1e-6)
     for rep in range(2):
         f, best = ev.evaluate(ph, ep, sz, 1e-6)
