@@ -389,7 +389,7 @@ def run_batch(args):
     block, grid, rows, tune = be.shape()
     kernel_ms = float(np.mean(step_ms))
     cpu_v, cpu_n, cpu_cores, cpu_t = batch_cpu_sample(pops, sym, args.cpu_fraction)
-    issue = profile_value("eval_batch_kernel_uneven-batch-small", "issue_active_frac")
+    issue = profile_value("eval_batch_kernel_uneven-batch-mid", "issue_active_frac")
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup,
