@@ -351,25 +351,19 @@ __device__ int2 translate_program(const TranslateArgs& ta, int i, int sz, const 
    return make_int2(kKindGeneric | (1 << 8), sz + 2);
 }
 
-// Shared-memory layout of the translator (SMEM = true): per thread, its
-// program's tokens and ephemerals and the scratch of both passes, with odd
-// per-thread strides so that threads at the same step hit different banks.
-__host__ __device__ inline int translate_stride(int max_size) { return max_size | 1; }
-__host__ __device__ inline size_t translate_smem_per_thread(int max_size) {
-   const int s1 = translate_stride(max_size);
-   return (size_t)s1 * (4 + 4 + 8) + (size_t)(2 * max_size + 1) * 4;
-}
-constexpr int kTranslateSmemBlock = 32;
+// Shared memory of one program's translation (WARP = true): its tokens and
+// ephemerals, the node words and both passes' frames.
+__host__ __device__ inline size_t translate_smem_bytes(int max_size) { return (size_t)max_size * 24 + 16; }
 constexpr size_t kTranslateSmemMax = 200 * 1024;
 
-// One thread per program (WARP = false) or one warp per program, lane 0
-// walking it (WARP = true: for populations resident in one wave, where the
-// walks of 32 different programs in one warp would diverge and run one after
-// another).  SMEM: the CTA first copies its programs' tokens into shared
-// memory with coalesced loads and keeps both passes' scratch there (the
-// translation is a serial walk per program: in global memory each step would
-// wait on a cache miss); else the scratch is the global work array.
-template <int MATH, bool SMEM, bool WARP>
+// One warp per program (WARP = true: populations resident in one wave): the
+// warp copies the program's tokens into shared memory with coalesced loads
+// and lane 0 walks it there (the translation is a serial walk per program;
+// one thread per program would put 32 different walks in one warp, which
+// diverge and run one after another).  One thread per program (WARP = false:
+// larger populations, whose many resident warps hide the latency) with the
+// scratch in the global work array.
+template <int MATH, bool WARP>
 __global__ void translate_kernel(const TranslateArgs a) {
    extern __shared__ __align__(16) unsigned char tsmem[];
    if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -401,27 +395,6 @@ __global__ void translate_kernel(const TranslateArgs a) {
       eph = s_eph;
       w = s_w;
       frames = s_fr;
-   } else if constexpr (SMEM) {
-      i = blockIdx.x * blockDim.x + threadIdx.x;
-      const int B = blockDim.x, t = threadIdx.x, s1 = translate_stride(ms);
-      int32_t* s_ph = reinterpret_cast<int32_t*>(tsmem);
-      float* s_eph = reinterpret_cast<float*>(s_ph + (size_t)B * s1);
-      uint2* s_w = reinterpret_cast<uint2*>(s_eph + (size_t)B * s1);
-      uint32_t* s_fr = reinterpret_cast<uint32_t*>(s_w + (size_t)B * s1);
-      const int first = blockIdx.x * B;
-      const int count = min(B, a.n - first);
-      const int32_t* g_ph = a.phenotype + (size_t)first * ms;
-      const float* g_eph = a.ephemeral + (size_t)first * ms;
-      for (int e = t; e < count * ms; e += B) {
-         const int p = e / ms, k = e - p * ms;
-         s_ph[p * s1 + k] = g_ph[e];
-         s_eph[p * s1 + k] = g_eph[e];
-      }
-      __syncthreads();
-      ph = s_ph + (size_t)t * s1;
-      eph = s_eph + (size_t)t * s1;
-      w = s_w + (size_t)t * s1;
-      frames = s_fr + (size_t)t * (2 * ms + 1);
    } else {
       i = blockIdx.x * blockDim.x + threadIdx.x;
       ph = a.phenotype + (size_t)i * ms;
@@ -459,13 +432,13 @@ __global__ void translate_kernel(const TranslateArgs a) {
 
 template <int MATH>
 cudaError_t launch_translate_math(const TranslateArgs& a, cudaStream_t s, int sm_count) {
-   const size_t per_prog = translate_smem_per_thread(a.max_size) + 16;
+   const size_t per_prog = translate_smem_bytes(a.max_size);
    if (a.n <= sm_count * 64 && per_prog <= kTranslateSmemMax) {
       // a population resident in one wave: a warp per program
-      const cudaError_t e = cudaFuncSetAttribute(translate_kernel<MATH, true, true>,
+      const cudaError_t e = cudaFuncSetAttribute(translate_kernel<MATH, true>,
                                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)per_prog);
       if (e != cudaSuccess) return e;
-      translate_kernel<MATH, true, true><<<max(1, a.n), 32, per_prog, s>>>(a);
+      translate_kernel<MATH, true><<<max(1, a.n), 32, per_prog, s>>>(a);
       return cudaGetLastError();
    }
    // larger populations: a thread per program, scratch in global memory (many
@@ -473,7 +446,7 @@ cudaError_t launch_translate_math(const TranslateArgs& a, cudaStream_t s, int sm
    // shared memory left one warp per SM for 256-token programs, measured 3 %
    // slower on the uneven batch)
    const int grid = max(1, (a.n + 127) / 128);
-   translate_kernel<MATH, false, false><<<grid, 128, 0, s>>>(a);
+   translate_kernel<MATH, false><<<grid, 128, 0, s>>>(a);
    return cudaGetLastError();
 }
 

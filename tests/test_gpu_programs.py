@@ -233,3 +233,34 @@ def test_wide_dataset_staged_and_direct_columns(gpu_lib, oracle_lib, strat, lane
     pred = ev.predict(ph[-1], ep[-1], int(sz[-1]))
     assert_bitexact(pred, oracle_for(oracle_lib, d, rows=rows).predict(ph[-1], ep[-1], int(sz[-1])),
                     "predict")
+
+
+def test_large_population_thread_per_program_translator(gpu_lib, oracle_lib):
+    """12,000 programs: more than one wave of warps (64 x SMs on a GB300), so
+    the translator runs a thread per program with its scratch in global
+    memory (smaller populations get a warp per program); bit-exact against
+    the oracle, every opcode."""
+    d = load_golden("allops")
+    rng = np.random.default_rng(31)
+    rows = _dataset(rng, 200, d["rows"].shape[1] - 1)
+    gen = ProgramGen(d, rng, rows.shape[1])
+    progs = [gen.random(int(k)) for k in rng.integers(0, 25, 12000)]
+    ph, ep, sz = ProgramGen.rows(progs, 64)
+    _check(oracle_lib, d, rows, ph, ep, sz, "PDP", 0)
+
+
+def test_population_in_one_wave_runs_without_wide_pass(gpu_lib, oracle_lib):
+    """A population resident in one wave gets the main tile with every row its
+    programs can need (here all 4 columns, the target and the slots): the
+    evaluation is the translator and one evaluator launch, bit-exact."""
+    d = load_golden("allops")
+    rng = np.random.default_rng(32)
+    rows = _dataset(rng, 500, d["rows"].shape[1] - 1)
+    gen = ProgramGen(d, rng, rows.shape[1])
+    progs = [gen.random(int(k)) for k in rng.integers(0, 40, 300)]
+    ph, ep, sz = ProgramGen.rows(progs, 64)
+    ev = make_evaluator(d, "PDP", 0, "parity", population=len(sz), max_size=64, rows=rows)
+    f, _ = ev.evaluate(ph, ep, sz, 1e-6)
+    assert ev.last_launch_count() == 2
+    assert_bitexact(f, oracle_for(oracle_lib, d, rows=rows).evaluate(ph, ep, sz, "PDP", ev.lanes, 1e-6),
+                    "one wave")
