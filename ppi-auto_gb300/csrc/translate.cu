@@ -96,7 +96,9 @@ __device__ float fold(int op, float x0, float x1, float x2, int prot) {
 __device__ __forceinline__ bool is_const_leaf(int op) { return op == PPI_OP_CONST || op == PPI_OP_LITERAL; }
 
 // Translation of program i (valid size): writes its code, returns its meta.
-template <int MATH>
+// MAPPED: ph / eph already hold each token's op and immediate bits (mapped
+// by the whole warp before the walk); else the Symbols and ephemerals.
+template <int MATH, bool MAPPED>
 __device__ int2 translate_program(const TranslateArgs& ta, int i, int sz, const int32_t* ph, const float* eph,
                                   uint2* w, uint32_t* frames) {
    uint2* code = ta.code + (size_t)i * ta.code_stride;
@@ -107,7 +109,12 @@ __device__ int2 translate_program(const TranslateArgs& ta, int i, int sz, const 
    for (int k = sz - 1; k >= 0; --k) {
       int op;
       uint32_t imm;
-      map_token(ta, ph[k], eph[k], &op, &imm);
+      if constexpr (MAPPED) {
+         op = ph[k];
+         imm = __float_as_uint(eph[k]);
+      } else {
+         map_token(ta, ph[k], eph[k], &op, &imm);
+      }
       const int ar = op_arity(op);
       int before = depth;
       if (before < ar) { malformed = true; before = ar; }   // missing operands read as NaN
@@ -344,7 +351,12 @@ __device__ int2 translate_program(const TranslateArgs& ta, int i, int sz, const 
    for (int k = sz - 1; k >= 0; --k) {    // the original tokens: nothing folded
       int op;
       uint32_t imm;
-      map_token(ta, ph[k], eph[k], &op, &imm);
+      if constexpr (MAPPED) {
+         op = ph[k];
+         imm = __float_as_uint(eph[k]);
+      } else {
+         map_token(ta, ph[k], eph[k], &op, &imm);
+      }
       code[1 + sz - 1 - k] = make_uint2((uint32_t)op, imm);
    }
    code[1 + sz] = make_uint2(kGenericEnd, 0u);
@@ -377,7 +389,8 @@ __global__ void translate_kernel(const TranslateArgs a) {
    uint32_t* frames;
    int i;
    if constexpr (WARP) {
-      // one program per 32-thread CTA: all lanes copy, lane 0 translates
+      // one program per 32-thread CTA: all lanes copy and map the tokens,
+      // lane 0 translates
       i = blockIdx.x;
       int32_t* s_ph = reinterpret_cast<int32_t*>(tsmem);
       float* s_eph = reinterpret_cast<float*>(s_ph + ms);
@@ -385,9 +398,14 @@ __global__ void translate_kernel(const TranslateArgs a) {
       uint32_t* s_fr = reinterpret_cast<uint32_t*>(s_w + ms);
       if (i >= a.n) return;
       const int sz_all = min(max(a.size[i], 0), ms);
+      TranslateArgs tm = a;   // the mapping needs the program's dataset width
+      if (a.pop_of) tm.ncol = a.pops[a.pop_of[i]].ncol;
       for (int k = threadIdx.x; k < sz_all; k += blockDim.x) {
-         s_ph[k] = a.phenotype[(size_t)i * ms + k];
-         s_eph[k] = a.ephemeral[(size_t)i * ms + k];
+         int op;
+         uint32_t imm;
+         map_token(tm, a.phenotype[(size_t)i * ms + k], a.ephemeral[(size_t)i * ms + k], &op, &imm);
+         s_ph[k] = op;
+         s_eph[k] = __uint_as_float(imm);
       }
       __syncwarp();
       if (threadIdx.x != 0) return;
@@ -414,7 +432,7 @@ __global__ void translate_kernel(const TranslateArgs a) {
       nlin = pd.nlin;
    }
    const bool valid = sz > 0 && sz <= a.max_size;   // sizes outside [1, max_size] are size 0
-   const int2 m = valid ? translate_program<MATH>(ta, i, sz, ph, eph, w, frames) : make_int2(kKindInvalid, 0);
+   const int2 m = valid ? translate_program<MATH, WARP>(ta, i, sz, ph, eph, w, frames) : make_int2(kKindInvalid, 0);
    a.meta[i] = m;
    const int kind = meta_kind(m);
    const unsigned long long work = valid ? (unsigned long long)sz * (unsigned long long)nlin : 0ull;
