@@ -85,6 +85,7 @@ struct BatchGeo {
    int rows_wide = 1, grid_wide = 1;
    size_t smem_wide = 0;
    bool wide = false;
+   int wide_kernel = 1;                // 2: every population PP or PDP (whole-quad direct reads)
 };
 
 struct ppi_batch {
@@ -205,11 +206,15 @@ ppi_status batch_geometry(ppi_batch* b, int P, int rows_req, BatchGeo* g) {
       while (rows < fit && occupancy(direct, rows + 1) >= top) ++rows;
       return rows;
    };
-   if (occupancy(0, 1) < 1 || occupancy(1, 1) < 1)
+   // DP tiles start at any record: their direct reads need the ragged path
+   int wk = 2;
+   for (const PopDesc& p : b->host_pops)
+      if (p.strategy == PPI_STRATEGY_DP) wk = 1;
+   if (occupancy(0, 1) < 1 || occupancy(wk, 1) < 1)
       return bfail(b, PPI_ERR_UNSUPPORTED, "evaluator does not fit on an SM");
    int rows = best_rows(0);
    if (rows_req > 0) rows = std::min(rows_req, fit);
-   const int rows2 = std::max(best_rows(1), std::min(fit, kSlots + 1));
+   const int rows2 = std::max(best_rows(wk), std::min(fit, kSlots + 1));
    g->block = P;
    g->fit = fit;
    g->rows = rows;
@@ -219,8 +224,9 @@ ppi_status batch_geometry(ppi_batch* b, int P, int rows_req, BatchGeo* g) {
    g->grid = std::max(1, std::min(b->total, g->per_sm * b->sm_count));
    g->rows_wide = rows2;
    g->smem_wide = smem_for(rows2);
-   g->grid_wide = std::max(1, std::min(b->total, std::max(1, occupancy(1, rows2)) * b->sm_count));
+   g->grid_wide = std::max(1, std::min(b->total, std::max(1, occupancy(wk, rows2)) * b->sm_count));
    g->wide = rows < rows_max;
+   g->wide_kernel = wk;
    return PPI_OK;
 }
 
@@ -251,7 +257,7 @@ ppi_status enqueue_step(ppi_batch* b, const int32_t* ph, const float* eph, const
    b->last_launches = 4;   // translate, order scan, order scatter, main pass
    if (g.wide) {
       a.rows = g.rows_wide; a.wide_pass = 1;
-      PPI_BCUDA(b, launch_evaluate_batch(b->math, b->opset, 1, a, g.block, g.grid_wide, g.smem_wide, s));
+      PPI_BCUDA(b, launch_evaluate_batch(b->math, b->opset, g.wide_kernel, a, g.block, g.grid_wide, g.smem_wide, s));
       b->last_launches = 5;
    }
    return PPI_OK;
@@ -282,48 +288,60 @@ std::vector<int> row_levels(ppi_batch* b, int P) {
 // warp as the best 128-thread shape.
 ppi_status autotune(ppi_batch* b, const int32_t* ph, const float* eph, const int32_t* size, float* fit,
                     int32_t* best, cudaStream_t s) {
-   auto time_shape = [&](const BatchGeo& g, float* ms) -> ppi_status {
-      ppi_status st = enqueue_step(b, ph, eph, size, fit, best, s, g);   // warm
+   auto time_once = [&](const BatchGeo& g, float* ms) -> ppi_status {
+      PPI_BCUDA(b, cudaEventRecord(b->ev0, s));
+      ppi_status st = enqueue_step(b, ph, eph, size, fit, best, s, g);
       if (st != PPI_OK) return st;
-      float t = 0.0f;
-      for (int rep = 0; rep < 2; ++rep) {
-         PPI_BCUDA(b, cudaEventRecord(b->ev0, s));
-         st = enqueue_step(b, ph, eph, size, fit, best, s, g);
-         if (st != PPI_OK) return st;
-         PPI_BCUDA(b, cudaEventRecord(b->ev1, s));
-         PPI_BCUDA(b, cudaEventSynchronize(b->ev1));
-         float one = 0.0f;
-         PPI_BCUDA(b, cudaEventElapsedTime(&one, b->ev0, b->ev1));
-         t = rep == 0 ? one : std::min(t, one);
-         if (one > 50.0f) break;   // long steps: one timing is enough
-      }
-      *ms = t;
+      PPI_BCUDA(b, cudaEventRecord(b->ev1, s));
+      PPI_BCUDA(b, cudaEventSynchronize(b->ev1));
+      PPI_BCUDA(b, cudaEventElapsedTime(ms, b->ev0, b->ev1));
       return PPI_OK;
    };
-   BatchGeo best_g;
-   float best_ms = -1.0f;
-   b->tune_ms[0] = b->tune_ms[1] = -1.0f;
+   // candidates: 128-thread CTAs at the most rows of each of the best
+   // occupancy levels, then 64-thread CTAs with twice the rows of the best
+   // 128-thread shape (the same shared memory per warp)
+   std::vector<BatchGeo> cand;
    for (int r : row_levels(b, 128)) {
       BatchGeo g;
-      if (batch_geometry(b, 128, r, &g) != PPI_OK) continue;
-      float ms;
-      ppi_status st = time_shape(g, &ms);
-      if (st != PPI_OK) return st;
-      if (b->tune_ms[1] < 0.0f || ms < b->tune_ms[1]) b->tune_ms[1] = ms;
-      if (best_ms < 0.0f || ms < best_ms) { best_ms = ms; best_g = g; }
+      if (batch_geometry(b, 128, r, &g) == PPI_OK) cand.push_back(g);
    }
-   // 64-thread CTAs: twice the rows of the best 128-thread shape fit in the
-   // same shared memory per warp
+   if (cand.empty()) return bfail(b, PPI_ERR_UNSUPPORTED, "no block shape fits this batch");
+   // Each candidate is timed in two round-robin rounds after one warm step,
+   // and keeps its faster time: a single timing in a fixed order favoured the
+   // later shapes while the clocks were still rising.
+   std::vector<float> best_of(cand.size(), -1.0f);
+   auto rounds = [&](size_t from) -> ppi_status {
+      for (size_t c = from; c < cand.size(); ++c) {
+         float ms;
+         ppi_status st = enqueue_step(b, ph, eph, size, fit, best, s, cand[c]);   // warm
+         if (st != PPI_OK) return st;
+         if ((st = time_once(cand[c], &ms)) != PPI_OK) return st;
+         best_of[c] = ms;
+      }
+      for (size_t c = from; c < cand.size(); ++c) {
+         float ms;
+         ppi_status st = time_once(cand[c], &ms);
+         if (st != PPI_OK) return st;
+         best_of[c] = std::min(best_of[c], ms);
+      }
+      return PPI_OK;
+   };
+   ppi_status st = rounds(0);
+   if (st != PPI_OK) return st;
+   size_t pick = 0;
+   for (size_t c = 1; c < cand.size(); ++c)
+      if (best_of[c] < best_of[pick]) pick = c;
+   b->tune_ms[1] = best_of[pick];
+   b->tune_ms[0] = -1.0f;
    BatchGeo g64;
-   if (batch_geometry(b, 64, best_ms < 0.0f ? 0 : 2 * best_g.rows, &g64) == PPI_OK) {
-      float ms;
-      ppi_status st = time_shape(g64, &ms);
-      if (st != PPI_OK) return st;
-      b->tune_ms[0] = ms;
-      if (best_ms < 0.0f || ms < best_ms) { best_ms = ms; best_g = g64; }
+   if (batch_geometry(b, 64, 2 * cand[pick].rows, &g64) == PPI_OK) {
+      cand.push_back(g64);
+      best_of.push_back(-1.0f);
+      if ((st = rounds(cand.size() - 1)) != PPI_OK) return st;
+      b->tune_ms[0] = best_of.back();
+      if (best_of.back() < best_of[pick]) pick = cand.size() - 1;
    }
-   if (best_ms < 0.0f) return bfail(b, PPI_ERR_UNSUPPORTED, "no block shape fits this batch");
-   b->geo = best_g;
+   b->geo = cand[pick];
    b->tuned = true;
    return PPI_OK;
 }

@@ -168,7 +168,8 @@ const char* plan_geometry(int strategy, int lanes, int math, int opset, int nlin
    }
    // second pass: the rest, with the columns that do not fit read directly
    // (room at least for the deepest slot need and the target)
-   const int rows2 = std::max(best_rows(1), std::min(fit, kSlots + 1));
+   const int wk = strategy == PPI_STRATEGY_DP ? 1 : 2;   // DP tiles start at any record
+   const int rows2 = std::max(best_rows(wk), std::min(fit, kSlots + 1));
    g->lanes = L;
    g->block = P;
    g->R = R;
@@ -182,7 +183,8 @@ const char* plan_geometry(int strategy, int lanes, int math, int opset, int nlin
    g->wide = rows < rows_max;
    g->rows_wide = rows2;
    g->smem_wide = evaluate_smem_bytes(code_stride, rows2, P, R, L, aligned);
-   g->per_sm[1] = occupancy(1, rows2);
+   g->wide_kernel = wk;
+   g->per_sm[1] = occupancy(wk, rows2);
    if (g->per_sm[1] < 1) return "evaluator does not fit on an SM";
    g->grid_wide = std::max(1, std::min(n_max, g->per_sm[1] * sm_count));
    return nullptr;

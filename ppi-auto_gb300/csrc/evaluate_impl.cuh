@@ -64,7 +64,10 @@ struct Direct {
 // x = the operand of an instruction: tile row `imm`, or with kDirectColumn the
 // record column read from global memory (positions at or past ld read 0, as a
 // staged row has them).  Kernels built with D = 0 run only programs whose
-// columns are all staged, and carry no code for direct reads.
+// columns are all staged, and carry no code for direct reads; D = 2 reads
+// whole 16-byte quads only (tiles of PP and PDP), D = 1 also the ragged ones
+// (DP tiles start at any record).  The scalar path's code, unused in PP and
+// PDP, cost the wide pass 7 % (instruction-cache misses) before D = 2.
 template <int D, int R>
 __device__ __forceinline__ void load_operand(uint32_t imm, const float* mine, int T, int P, int tid,
                                              const Direct& g, float (&x)[R]) {
@@ -76,7 +79,20 @@ __device__ __forceinline__ void load_operand(uint32_t imm, const float* mine, in
 #pragma unroll
    for (int i = 0; i < R / 4; ++i) {
       const int pos = (i * P + tid) * 4;
-      if (g.vec && pos + 3 < g.avail) {
+      if constexpr (D == 2) {
+         // whole quads only (every tile starts on a multiple of 4 records and
+         // ends inside the padded column: PP and PDP); the else branch is a
+         // guard that those tiles never take (this form measured 8 % faster
+         // on the uneven batch than a zero-initialised quad with a
+         // conditional load, or than the condition without g.vec)
+         if (g.vec && pos + 3 < g.avail) {
+            const float4 u = __ldg(reinterpret_cast<const float4*>(col + pos));
+            x[4 * i] = u.x; x[4 * i + 1] = u.y; x[4 * i + 2] = u.z; x[4 * i + 3] = u.w;
+         } else {
+#pragma unroll
+            for (int q = 0; q < 4; ++q) x[4 * i + q] = 0.0f;
+         }
+      } else if (g.vec && pos + 3 < g.avail) {
          const float4 u = __ldg(reinterpret_cast<const float4*>(col + pos));
          x[4 * i] = u.x; x[4 * i + 1] = u.y; x[4 * i + 2] = u.z; x[4 * i + 3] = u.w;
       } else {
@@ -686,13 +702,23 @@ struct Launch {
    using EvalFn = void (*)(const EvalArgs);
    using BatchFn = void (*)(const BatchArgs);
    using PredictFn = void (*)(const PredictArgs);
+   // direct: 0 the main pass, 1 the wide pass (any tile), 2 the wide pass
+   // (tiles of whole quads)
+   template <int OPSET>
+   static EvalFn eval_fn_set(int direct) {
+      return direct == 2 ? eval_kernel<MATH, kR, OPSET, 2>
+                         : (direct ? eval_kernel<MATH, kR, OPSET, 1> : eval_kernel<MATH, kR, OPSET, 0>);
+   }
+   template <int OPSET>
+   static BatchFn batch_fn_set(int direct) {
+      return direct == 2 ? eval_batch_kernel<MATH, kR, OPSET, 2>
+                         : (direct ? eval_batch_kernel<MATH, kR, OPSET, 1> : eval_batch_kernel<MATH, kR, OPSET, 0>);
+   }
    static EvalFn eval_fn(int opset, int direct) {
-      return opset ? (direct ? eval_kernel<MATH, kR, kOpsetArith, 1> : eval_kernel<MATH, kR, kOpsetArith, 0>)
-                   : (direct ? eval_kernel<MATH, kR, kOpsetFull, 1> : eval_kernel<MATH, kR, kOpsetFull, 0>);
+      return opset ? eval_fn_set<kOpsetArith>(direct) : eval_fn_set<kOpsetFull>(direct);
    }
    static BatchFn batch_fn(int opset, int direct) {
-      return opset ? (direct ? eval_batch_kernel<MATH, kR, kOpsetArith, 1> : eval_batch_kernel<MATH, kR, kOpsetArith, 0>)
-                   : (direct ? eval_batch_kernel<MATH, kR, kOpsetFull, 1> : eval_batch_kernel<MATH, kR, kOpsetFull, 0>);
+      return opset ? batch_fn_set<kOpsetArith>(direct) : batch_fn_set<kOpsetFull>(direct);
    }
    static PredictFn predict_fn(int opset) {
       return opset ? predict_kernel<MATH, kR, kOpsetArith> : predict_kernel<MATH, kR, kOpsetFull>;
@@ -702,7 +728,7 @@ struct Launch {
       static bool done[2] = {false, false};
       if (done[opset]) return cudaSuccess;
       const int attr = cudaFuncAttributeMaxDynamicSharedMemorySize, bytes = 200 * 1024;
-      for (int direct = 0; direct < 2; ++direct) {
+      for (int direct = 0; direct < 3; ++direct) {
          cudaError_t e = cudaFuncSetAttribute(eval_fn(opset, direct), (cudaFuncAttribute)attr, bytes);
          if (e == cudaSuccess) e = cudaFuncSetAttribute(batch_fn(opset, direct), (cudaFuncAttribute)attr, bytes);
          if (e != cudaSuccess) return e;

@@ -178,7 +178,7 @@ extern "C" ppi_status ppi_gpu_evaluate_noalloc(const ppi_gpu_config* c, const fl
    if (launch_evaluate(c->math, g.opset, 0, e, g.block, g.grid, g.smem, s) != cudaSuccess) return PPI_ERR_CUDA;
    if (g.wide) {
       e.rows = g.rows_wide; e.wide_pass = 1; e.final_pass = 1;
-      if (launch_evaluate(c->math, g.opset, 1, e, g.block, g.grid_wide, g.smem_wide, s) != cudaSuccess)
+      if (launch_evaluate(c->math, g.opset, g.wide_kernel, e, g.block, g.grid_wide, g.smem_wide, s) != cudaSuccess)
          return PPI_ERR_CUDA;
    }
    return PPI_OK;

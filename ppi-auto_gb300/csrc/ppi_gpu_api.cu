@@ -167,7 +167,7 @@ ppi_status enqueue(ppi_gpu* h, const int32_t* d_ph, const float* d_eph, const in
    h->last_launches = 2;
    if (g.wide) {
       e.rows = g.rows_wide; e.wide_pass = 1; e.final_pass = 1;
-      PPI_CUDA(h, launch_evaluate(h->cfg.math, g.opset, 1, e, g.block, std::min(g.grid_wide, n),
+      PPI_CUDA(h, launch_evaluate(h->cfg.math, g.opset, g.wide_kernel, e, g.block, std::min(g.grid_wide, n),
                                   g.smem_wide, s));
       h->last_launches = 3;
    }

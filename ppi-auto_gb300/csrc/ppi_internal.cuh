@@ -450,6 +450,7 @@ struct Geometry {
    bool wide = false;
    bool aligned = false;
    int per_sm[2] = {0, 0};     // resident CTAs per SM of the two passes
+   int wide_kernel = 1;        // direct-read kernel of the wide pass: 2 whole quads (PP, PDP), 1 any tile
 };
 // kOpsetArith when every op of the symbol table is in the ARITH set.
 int opset_for(const ppi_symbol_entry* symbols, int n);
