@@ -168,7 +168,11 @@ const char* plan_geometry(int strategy, int lanes, int math, int opset, int nlin
    }
    // second pass: the rest, with the columns that do not fit read directly
    // (room at least for the deepest slot need and the target)
-   const int wk = strategy == PPI_STRATEGY_DP ? 1 : 2;   // DP tiles start at any record
+   // whole-quad direct reads need tiles that start on a multiple of 4
+   // records: PP and PDP tiles (T records) always do, DP tiles (L * (T / L))
+   // when that is a multiple of 4
+   const int tile_step = strategy == PPI_STRATEGY_DP ? L * ((P * R) / L) : P * R;
+   const int wk = tile_step % 4 == 0 ? 2 : 1;
    const int rows2 = std::max(best_rows(wk), std::min(fit, kSlots + 1));
    g->lanes = L;
    g->block = P;

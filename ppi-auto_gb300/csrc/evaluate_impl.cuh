@@ -65,8 +65,8 @@ struct Direct {
 // record column read from global memory (positions at or past ld read 0, as a
 // staged row has them).  Kernels built with D = 0 run only programs whose
 // columns are all staged, and carry no code for direct reads; D = 2 reads
-// whole 16-byte quads only (tiles of PP and PDP), D = 1 also the ragged ones
-// (DP tiles start at any record).  The scalar path's code, unused in PP and
+// whole 16-byte quads only (tiles that start on a multiple of 4 records: PP,
+// PDP, and DP when lanes * (T / lanes) is one), D = 1 also the ragged ones.  The scalar path's code, unused in PP and
 // PDP, cost the wide pass 7 % (instruction-cache misses) before D = 2.
 template <int D, int R>
 __device__ __forceinline__ void load_operand(uint32_t imm, const float* mine, int T, int P, int tid,
@@ -80,11 +80,11 @@ __device__ __forceinline__ void load_operand(uint32_t imm, const float* mine, in
    for (int i = 0; i < R / 4; ++i) {
       const int pos = (i * P + tid) * 4;
       if constexpr (D == 2) {
-         // whole quads only (every tile starts on a multiple of 4 records and
-         // ends inside the padded column: PP and PDP); the else branch is a
-         // guard that those tiles never take (this form measured 8 % faster
-         // on the uneven batch than a zero-initialised quad with a
-         // conditional load, or than the condition without g.vec)
+         // whole quads only: every tile starts on a multiple of 4 records and
+         // the padded column length is one, so a quad is either inside the
+         // column or past its end (read as 0 by the else branch).  This form
+         // measured 8 % faster on the uneven batch than a zero-initialised
+         // quad with a conditional load, or than the condition without g.vec.
          if (g.vec && pos + 3 < g.avail) {
             const float4 u = __ldg(reinterpret_cast<const float4*>(col + pos));
             x[4 * i] = u.x; x[4 * i + 1] = u.y; x[4 * i + 2] = u.z; x[4 * i + 3] = u.w;
