@@ -204,8 +204,12 @@ def run_reference(args):
         return 0
     from oracle import pyoracle
     pyoracle.build()
-    if args.workload == "polynomial":
-        return run_reference_polynomial(args)
+    if args.workload in ("polynomial", "iris", "stream"):
+        return run_reference_single(args)
+    if args.workload == "adjoint":
+        print(json.dumps({"impl": "reference", "unavailable":
+                          "the reference has no constant adjoint (PPI evaluates fitness only)"}))
+        return 0
     from ppi_gpu import workloads
     g, pops = workloads.uneven_batch(seed=11, n_pops=args.populations,
                                      pop_range=(256, args.max_programs))
@@ -238,17 +242,25 @@ def run_reference(args):
     return 0
 
 
-def run_reference_polynomial(args):
+def run_reference_single(args):
+    """The reference arm of the single-population workloads: the oracle port of
+    the reference's CPU interpreter on the same workload as `run_polynomial`,
+    each step a slice of the population (all records)."""
     from ppi_gpu import workloads
     from oracle import pyoracle
-    wl = workloads.polynomial()
+    if args.workload == "polynomial":
+        wl, per_step = workloads.polynomial(nlin=args.records, population=args.population), 60
+    elif args.workload == "iris":
+        wl = workloads.iris_shaped(population=args.population)
+        per_step = wl.population   # the whole population: a few ms of CPU work
+    else:
+        wl, per_step = workloads.streaming(nlin=args.records, population=args.population), 48
     ph, eph, sz = pyoracle.decode(wl.grammar, wl.genomes, wl.bits_per_gene,
                                   wl.bits_per_constant, wl.lo, wl.hi, wl.max_size)
-    # each step: a bounded sample (a fixed slice of the population, all records)
-    per_step = 60
+    per_step = min(per_step, len(sz))
     vals = []
     for k in range(args.warmup + args.steps):
-        lo = (k * per_step) % (len(sz) - per_step)
+        lo = (k * per_step) % max(1, len(sz) - per_step + 1)
         v, n, cores, t = cpu_sample(wl, ph[lo:lo + per_step], eph[lo:lo + per_step],
                                     sz[lo:lo + per_step], 0.0, 0, per_step)
         if k >= args.warmup:
@@ -673,13 +685,13 @@ def main():
     ap.add_argument("--population", type=int, default=30_000)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
+    if args.workload == "stream" and args.records == 100_000:
+        args.records = 4_000_000
+    if args.workload == "iris" and args.population == 30_000:
+        args.population = 1000
     if args.impl == "reference":
         return run_reference(args)
     if args.workload in ("polynomial", "iris", "stream"):
-        if args.workload == "stream" and args.records == 100_000:
-            args.records = 4_000_000
-        if args.workload == "iris" and args.population == 30_000:
-            args.population = 1000
         return run_polynomial(args)
     if args.workload == "adjoint":
         return run_adjoint(args)
