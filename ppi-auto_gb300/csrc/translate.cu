@@ -280,6 +280,10 @@ __device__ int2 translate_program(const TranslateArgs& ta, int i, int sz, const 
          const int c1 = c0 + node_sub(w[c0]);
          if (ar == 2) {
             const uint32_t bo = (uint32_t)(op - PPI_OP_AND);
+            // + and x are commutative bit for bit in IEEE arithmetic: their
+            // operand-first forms (_R) become accumulator-first ones (_L), so
+            // fewer distinct cases run hot in the interpreter
+            const bool comm = op == PPI_OP_ADD || op == PPI_OP_MULT;
             const bool l0 = is_leaf(c0), l1 = is_leaf(c1);
             if (l0 && l1) {
                emit(leaf_attr(c0) ? M_LD_ROW : M_LD_C, w[c0].y);
@@ -290,7 +294,7 @@ __device__ int2 translate_program(const TranslateArgs& ta, int i, int sz, const 
                else { emit((leaf_attr(c1) ? M_BR_L : M_BC_L) + bo, w[c1].y); --fp; }
             } else if (l0) {
                if (st == 0) { frames[fp - 1] = frame(node, d, 1); frames[fp++] = frame(c1, d, 0); }
-               else { emit((leaf_attr(c0) ? M_BR_R : M_BC_R) + bo, w[c0].y); --fp; }
+               else { emit((leaf_attr(c0) ? (comm ? M_BR_L : M_BR_R) : (comm ? M_BC_L : M_BC_R)) + bo, w[c0].y); --fp; }
             } else {
                const bool left_first = node_need(w[c0]) >= node_need(w[c1]);
                const int first = left_first ? c0 : c1, second = left_first ? c1 : c0;
@@ -303,7 +307,7 @@ __device__ int2 translate_program(const TranslateArgs& ta, int i, int sz, const 
                   frames[fp++] = frame(second, d + 1, 0);
                } else {
                   // slot d holds `first`, acc holds `second`
-                  emit((left_first ? M_BR_R : M_BR_L) + bo, slot0 + (uint32_t)d);
+                  emit((left_first && !comm ? M_BR_R : M_BR_L) + bo, slot0 + (uint32_t)d);
                   --fp;
                }
             }
