@@ -36,7 +36,7 @@
 extern "C" {
 #endif
 
-#define PPI_GPU_ABI_VERSION 1
+#define PPI_GPU_ABI_VERSION 2
 
 typedef enum {
    PPI_OK = 0,
@@ -103,6 +103,21 @@ typedef struct {
    float value;
 } ppi_symbol_entry;
 
+/* Which program the best index names (the `index` output of acc_interpret).
+ *   ACCELERATOR (default): what src/interpreter/accelerator.cc returns.  The
+ *     best_individual kernel (accelerator.cl:271-313) reduces work-groups of
+ *     `best_group` programs by a strided tree that keeps the left value on
+ *     ties, and util::PickNBest (src/util/Util.h:158-173) then takes the
+ *     smallest group winner, ties to the largest group
+ *     (accelerator.cc:871-880).  PP and PDP compare the alpha-free values
+ *     error/nlin (kernel2 reads buffer_vector before the host adds
+ *     alpha*size, accelerator.cc:500,720,848-849); DP compares the fitness
+ *     with alpha*size (buffer_error, accelerator.cc:491,801,812).
+ *   SEQUENTIAL: what src/interpreter/sequential.cc returns: PickNBest over
+ *     the fitness with alpha*size, ties to the largest index (:203).
+ * Both leave the fitness values unchanged. */
+typedef enum { PPI_BEST_ACCELERATOR = 0, PPI_BEST_SEQUENTIAL = 1 } ppi_best_rule;
+
 typedef struct {
    int32_t max_size;          /* MAX_PHENOTYPE_SIZE: row stride of phenotype/ephemeral  */
    int32_t population_size;   /* largest n given to evaluate                            */
@@ -118,6 +133,10 @@ typedef struct {
    const ppi_symbol_entry* symbols;
    int32_t n_symbols;
    int32_t device;            /* CUDA device ordinal                                    */
+   int32_t best_rule;         /* ppi_best_rule                                          */
+   int32_t best_group;        /* ACCELERATOR: programs per best_individual work-group;
+                                 <= 0 picks the reference's rule for a 152-CU device,
+                                 min(1024, ceil(population_size / CUs)) (accelerator.cc:348) */
 } ppi_gpu_config;
 
 typedef struct ppi_gpu ppi_gpu;
@@ -142,8 +161,7 @@ ppi_status ppi_gpu_set_dataset_rowmajor(ppi_gpu* h, const float* data, int32_t n
  * holds n program lengths (0 = invalid program).  fitness[i] receives
  * error/nlin + alpha*size[i] (FLT_MAX for invalid or non-finite programs, as
  * the reference strategy defines); *best_index (may be NULL) receives the
- * smallest fitness, ties resolved toward the largest index as
- * util::PickNBest does (src/util/Util.h:158-173). */
+ * best program under config->best_rule (ppi_best_rule above). */
 ppi_status ppi_gpu_evaluate(ppi_gpu* h, const int32_t* phenotype, const float* ephemeral,
                             const int32_t* size, int32_t n, float alpha, float* fitness,
                             int32_t* best_index);
@@ -201,6 +219,20 @@ int32_t ppi_gpu_lanes(const ppi_gpu* h);
 
 /* Number of kernel launches the last evaluate / predict / decode call made. */
 int32_t ppi_gpu_last_launch_count(const ppi_gpu* h);
+
+/* Inspection of the last evaluate call's translation (waits for it).  No
+ * reference counterpart: the bytecode is this library's own.  code_stride
+ * receives the uint2 words of one program's code; opset the opcode set of the
+ * kernels that run it (0 every opcode, 1 the arithmetic set); code (may be
+ * NULL) n * code_stride * 2 uint32 words; meta (may be NULL) n * 2 int32
+ * {kind | rows << 8, code length}.  n at most the last call's n. */
+ppi_status ppi_gpu_translation(ppi_gpu* h, int32_t n, uint32_t* code, int32_t* meta,
+                               int32_t* code_stride, int32_t* opset);
+
+/* Compute capability the evaluator kernels were compiled for, as loaded on
+ * the current device (cudaFuncAttributes::binaryVersion, 103 for sm_103a);
+ * -1 when no device is usable.  No reference counterpart: a build check. */
+int32_t ppi_gpu_kernel_arch(void);
 
 /* ---- constant adjoint --------------------------------------------------------
  * No counterpart in the reference: an addition for refining the ephemeral
@@ -283,20 +315,27 @@ ppi_status ppi_batch_set_shape(ppi_batch* b, int32_t block, int32_t rows);
  * d_data 16-byte aligned, target in the last column), the programs (rows of
  * config->max_size) and the outputs.  Work is queued on `stream` (a
  * cudaStream_t); the call does not synchronise.  config->population_size is
- * ignored; config->symbols and config->cost are read during the call.
+ * ignored (the automatic best_group uses n); config->symbols and config->cost
+ * are read from host memory by each call, with cudaMemcpyAsync.
  * Scratch comes from one fixed 64 MiB array inside the library, which every
  * GPU that loads the library holds until exit.  A batch needing more
- * (about 16,000 programs of max_size 128) is rejected with
- * PPI_ERR_UNSUPPORTED and a message on stderr.  The first call on each device
- * looks up the array's device address, so make it before any stream capture.
- * All calls share the array: calls that overlap on the GPU race, so
- * serialise them.  Programs the generic interpreter cannot hold get FLT_MAX
- * here without a status report. */
+ * (about 16,000 programs of max_size 128), or a symbol table spanning more
+ * than 2^22 values, is rejected with PPI_ERR_UNSUPPORTED and a message on
+ * stderr.  The first call on each device looks up the array's device address
+ * and caches the launch geometry, so make that first call before any stream
+ * capture.  All calls share the array: calls that overlap on the GPU race, so
+ * serialise them.  d_status (device memory, may be NULL) receives the
+ * kernels' status bits once the call's work is done: 0 when every program
+ * ran; 1 a malformed program needs a deeper stack than the generic
+ * interpreter's (its fitness is FLT_MAX); 2 a tile copy did not complete
+ * within its bounded wait; 4 an instruction outside the kernel's opcode set
+ * (the fitness values are not to be used after 2 or 4). */
 ppi_status ppi_gpu_evaluate_noalloc(const ppi_gpu_config* config, const float* d_data,
                                     int32_t nlin, int32_t ncol, int32_t ld,
                                     const int32_t* d_phenotype, const float* d_ephemeral,
                                     const int32_t* d_size, int32_t n, float alpha,
-                                    float* d_fitness, int32_t* d_best_index, void* stream);
+                                    float* d_fitness, int32_t* d_best_index, int32_t* d_status,
+                                    void* stream);
 
 #ifdef __cplusplus
 }

@@ -23,7 +23,9 @@ reference's own -DEF mechanism, because ``COST[(int)X][(int)Y]`` indexes out of
 bounds whenever a prediction is not a class index: NaN X gives a NaN error and
 each index is (int)v clamped to [0, N).
 
-Usage: python3 oracle/build_ref.py [--ref /root/reference] [--only NAME ...]
+Usage: python3 oracle/build_ref.py [--ref TREE] [--only NAME ...]
+The tree is --ref, else $PPI_REFERENCE, else the reference checkout this
+recipe was written against (REFERENCE_DEFAULT).
 """
 import argparse
 import json
@@ -38,6 +40,13 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(HERE)
 OUT = os.path.join(HERE, "_ref")
 GRAMMARS = os.path.join(REPO, "ppi-auto_gb300", "grammars")
+REFERENCE_DEFAULT = "/root/reference"
+
+
+def reference_root():
+    """The reference tree this recipe and the tests that read reference
+    sources use: $PPI_REFERENCE when set, else REFERENCE_DEFAULT."""
+    return os.environ.get("PPI_REFERENCE", REFERENCE_DEFAULT)
 
 COST8 = ("[8]={{0,1.5,0.75,1.25,2,0.5,1,1.75},{1,0,1.5,0.5,0.75,2,1.25,0.6},"
          "{0.8,1.1,0,1.9,0.55,1.3,0.7,1.6},{1.4,0.65,1.2,0,1.05,0.9,1.8,0.5},"
@@ -154,7 +163,7 @@ def build_one(ref, name, spec):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=reference_root())
     ap.add_argument("--only", nargs="*")
     a = ap.parse_args()
     if not os.path.isdir(os.path.join(a.ref, "src", "interpreter")):

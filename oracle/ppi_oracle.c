@@ -384,6 +384,53 @@ int ppio_best_index(const float* f, int n) {
    return best;
 }
 
+/* The accelerator's best index: the best_individual kernel
+ * (src/interpreter/accelerator.cl:271-313) run with work-groups of `group`
+ * items over ceil(n / group) groups, each group reducing its values by the
+ * strided local tree that keeps the left operand unless it is strictly
+ * greater (:290-307), then util::PickNBest(1) over the groups' winners on the
+ * host (src/interpreter/accelerator.cc:871-880; src/util/Util.h:158-173):
+ * the smallest winner value, ties to the largest group.  Items past n read
+ * MAXFLOAT (:286); their index is never used here because a group winner is
+ * a padding item only when every real item of its group exceeds MAXFLOAT,
+ * which the callers' values (FLT_MAX sentinels for non-finite errors) never
+ * do.  Returns -1 when n or group is not positive. */
+int ppio_best_index_accelerator(const float* vec, int n, int group) {
+   if (n < 1 || group < 1) return -1;
+   const int groups = (n + group - 1) / group;
+   float* lo_best = (float*)malloc(sizeof(float) * (size_t)group);
+   int* lo_idx = (int*)malloc(sizeof(int) * (size_t)group);
+   float* pb = (float*)malloc(sizeof(float) * (size_t)groups);
+   int* pi = (int*)malloc(sizeof(int) * (size_t)groups);
+   if (!lo_best || !lo_idx || !pb || !pi) {
+      free(lo_best); free(lo_idx); free(pb); free(pi);
+      return -1;
+   }
+   /* next_power_of_2 of the kernel: pown(2, ceil(log2(lo_size))) / 2 */
+   int half = 1;
+   while (half < group) half <<= 1;
+   half >>= 1;
+   for (int g = 0; g < groups; ++g) {
+      for (int l = 0; l < group; ++l) {
+         const int gl = g * group + l;
+         lo_best[l] = gl < n ? vec[gl] : FLT_MAX;
+         lo_idx[l] = gl < n ? gl : -1;
+      }
+      for (int s = half; s > 0; s /= 2)
+         for (int l = 0; l < s; ++l)
+            if (l + s < group && lo_best[l] > lo_best[l + s]) {
+               lo_best[l] = lo_best[l + s];
+               lo_idx[l] = lo_idx[l + s];
+            }
+      pb[g] = lo_best[0];
+      pi[g] = lo_idx[0];
+   }
+   const int w = ppio_best_index(pb, groups);
+   const int best = pi[w];
+   free(lo_best); free(lo_idx); free(pb); free(pi);
+   return best;
+}
+
 /* ---- decode (src/ppi.cc:106-182) ---------------------------------------- */
 typedef struct {
    const int32_t *rule_first, *rule_count, *alt_len, *alt_syms;

@@ -51,6 +51,13 @@ int ppio_predict(const ppio_config* cfg, const int32_t* phenotype, const float* 
  * ties resolved toward the largest index. */
 int ppio_best_index(const float* fitness, int n);
 
+/* The best index acc_interpret returns: best_individual
+ * (src/interpreter/accelerator.cl:271-313) over work-groups of `group`
+ * values, then PickNBest(1) over the group winners
+ * (src/interpreter/accelerator.cc:871-880).  PP/PDP pass the alpha-free
+ * per-program values, DP the alpha-included fitness. */
+int ppio_best_index_accelerator(const float* values, int n, int group);
+
 /* Genome decode (src/ppi.cc:106-182).  Tables as returned by
  * ppi_gpu.grammar.Grammar.decode_tables().  genomes: n x nb bytes of 0/1.
  * Rows of phenotype/ephemeral hold max_size entries.  Returns 0. */

@@ -64,6 +64,7 @@ def lib():
                                     C.c_int, C.c_float, _fp]
         L.ppio_predict.argtypes = [C.POINTER(_Cfg), _ip, _fp, C.c_int, _fp]
         L.ppio_best_index.argtypes = [_fp, C.c_int]
+        L.ppio_best_index_accelerator.argtypes = [_fp, C.c_int, C.c_int]
         _dp = C.POINTER(C.c_double)
         L.ppio_adjoint64.argtypes = [C.POINTER(_Cfg), _ip, _dp, _ip, C.c_int, C.c_int, C.c_int, _dp,
                                      _dp]
@@ -127,6 +128,13 @@ class Oracle:
 def best_index(fitness):
     f = np.ascontiguousarray(fitness, np.float32)
     return lib().ppio_best_index(_f(f), len(f))
+
+
+def best_index_accelerator(values, group):
+    """acc_interpret's best index: best_individual over work-groups of
+    `group` values, then PickNBest over the group winners."""
+    v = np.ascontiguousarray(values, np.float32)
+    return lib().ppio_best_index_accelerator(_f(v), len(v), int(group))
 
 
 def decode(grammar, genomes, bits_per_gene, bits_per_constant, lo, hi, max_size):

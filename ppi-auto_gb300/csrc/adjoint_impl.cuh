@@ -278,12 +278,15 @@ __global__ void __launch_bounds__(128, 4) adjoint_kernel(const AdjointArgs a) {
       }
       const int first = chunk * a.chunk, end = min(a.nlin, first + a.chunk);
       int tiles = 0;
+      bool stop = false;
       for (int base = first; base < end; base += T) {
          __syncthreads();   // every thread is done with the previous tile's rows
-         ev::stage_tile(a.data, a.ncol, a.ld, s_code, s_tile, base, T, tid, P, st, a.status);
-         __syncthreads();
+         if (!ev::stage_tile(a.data, a.ncol, a.ld, s_code, s_tile, base, T, tid, P, st, a.status)) {
+            stop = true;   // the tile never arrived (status recorded)
+            break;
+         }
          float p[R];
-         ev::run_fast<MATH, R, OPSET, 0>(fwd, mine, T, P, tid, none, p, a.prot);
+         ev::run_fast<MATH, R, OPSET, 0>(fwd, mine, T, P, tid, none, p, a.prot, a.status);
          // error derivative: the root's adjoint
          float ys[R], g[R];
          load_row(mine + (size_t)trow * T, P, ys);
@@ -324,6 +327,7 @@ __global__ void __launch_bounds__(128, 4) adjoint_kernel(const AdjointArgs a) {
       }
       if (tid == 0) a.pbad[(size_t)prog * a.n_chunks + chunk] = s_bad;
       __syncthreads();
+      if (stop) break;   // staging failed: this CTA takes no more work
    }
 }
 

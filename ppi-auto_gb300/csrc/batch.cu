@@ -354,7 +354,8 @@ extern "C" {
 ppi_status ppi_batch_create(const ppi_gpu_config* c, int32_t n_pops, const ppi_batch_population* pops,
                             ppi_batch** out) {
    if (!c || !pops || !out || n_pops < 1 || c->max_size < 1 || c->max_size > 65535 || c->math < 0 ||
-       c->math > 2 || c->n_symbols < 0 || (c->n_symbols > 0 && !c->symbols))
+       c->math > 2 || c->n_symbols < 0 || (c->n_symbols > 0 && !c->symbols) ||
+       (c->best_rule != PPI_BEST_ACCELERATOR && c->best_rule != PPI_BEST_SEQUENTIAL))
       return PPI_ERR_INVALID_ARGUMENT;
    *out = nullptr;
    long long total = 0;
@@ -430,6 +431,10 @@ ppi_status ppi_batch_create(const ppi_gpu_config* c, int32_t n_pops, const ppi_b
       pd.cost = dc; pd.cost_n = q.error_fn == PPI_EF_COST ? q.cost_n : 0; pd.alpha = 0.0f;
       pd.prog_begin = begin; pd.n = q.n;
       if (pd.lanes < 1 || pd.lanes > kMaxLanes) return bail(PPI_ERR_UNSUPPORTED);
+      // each population is one acc_interpret call: its own best_individual geometry
+      if (best_geometry(c->best_rule, resolve_best_group(c->best_rule, c->best_group, q.n, b->sm_count),
+                        q.strategy, q.n, &pd.best))
+         return bail(PPI_ERR_UNSUPPORTED);
       b->host_pops.push_back(pd);
       for (int i = 0; i < q.n; ++i) pop_of[(size_t)begin + i] = p;
       begin += q.n;
@@ -544,6 +549,8 @@ ppi_status ppi_batch_evaluate(ppi_batch* b, const int32_t* ph, const float* eph,
    cudaEventElapsedTime(&b->last_ms, b->ev0, b->ev1);
    if (*b->h_status & kStatusStageTimeout)
       return bfail(b, PPI_ERR_DEVICE_STATUS, "a tile copy did not complete (bounded wait expired)");
+   if (*b->h_status & kStatusBadInstruction)
+      return bfail(b, PPI_ERR_DEVICE_STATUS, "a kernel met an instruction outside its opcode set");
    if (*b->h_status & kStatusUnsupportedProgram)
       return bfail(b, PPI_ERR_UNSUPPORTED, "a malformed program needs a deeper stack than supported");
    return PPI_OK;

@@ -106,6 +106,31 @@ int resolve_lanes(int strategy, int lanes, int nlin, int sm_count) {
    return lanes;
 }
 
+int resolve_best_group(int rule, int group, int population, int sm_count) {
+   if (rule == PPI_BEST_SEQUENTIAL) return 1;
+   if (group > 0) return group;
+   // local_size2 = min(max_local_size2, ceil(population_size / max_cu)), with
+   // max_local_size2 = 1024 (the work-group limit; 48 KB of local memory / 8
+   // bytes per item allows more)
+   const long long cu = std::max(1, sm_count);
+   return (int)std::max(1LL, std::min(1024LL, ((long long)std::max(1, population) + cu - 1) / cu));
+}
+
+const char* best_geometry(int rule, int group, int strategy, int n, BestGeo* out) {
+   if (rule != PPI_BEST_ACCELERATOR && rule != PPI_BEST_SEQUENTIAL) return "unknown best-index rule";
+   if (group < 1 || n < 1) return "best-index group size must be positive";
+   int bits = 0;
+   while (bits < 31 && (1LL << bits) < group) ++bits;
+   const long long groups = ((long long)n + group - 1) / group;
+   // the tie field holds (groups - 1) << bits | position in 32 bits
+   if ((groups << bits) > (1LL << 32)) return "best-index group geometry does not fit the 32-bit tie field";
+   out->group = group;
+   out->bits = bits;
+   out->groups = (int)groups;
+   out->alpha_free = rule == PPI_BEST_ACCELERATOR && strategy != PPI_STRATEGY_DP;
+   return nullptr;
+}
+
 const char* plan_geometry(int strategy, int lanes, int math, int opset, int nlin, int ncol,
                           int code_stride, int n_max, int sm_count, Geometry* g) {
    const int L = lanes;

@@ -165,9 +165,19 @@ __device__ constexpr bool roll_unary() {
 
 template <int MATH, int R, int OPSET, int D>
 __device__ __forceinline__ void run_fast(const uint2* __restrict__ code, float* mine, int T, int P,
-                                         int tid, const Direct& g, float (&acc)[R], int prot) {
-   if constexpr (OPSET == kOpsetArith) run_fast_arith<MATH, R, D>(code, mine, T, P, tid, g, acc, prot);
-   else run_fast_full<MATH, R, D>(code, mine, T, P, tid, g, acc, prot);
+                                         int tid, const Direct& g, float (&acc)[R], int prot,
+                                         int* status) {
+   if constexpr (OPSET == kOpsetArith) run_fast_arith<MATH, R, D>(code, mine, T, P, tid, g, acc, prot, status);
+   else run_fast_full<MATH, R, D>(code, mine, T, P, tid, g, acc, prot, status);
+}
+
+// Copies a program's code (meta.y words) into shared memory and puts an end
+// marker after it (the region holds code_stride + 1 words), so neither
+// interpreter can walk past the code.
+__device__ __forceinline__ void load_code(uint2* s_code, const uint2* code, int2 meta, int tid, int P) {
+   for (int i = tid; i < meta.y; i += P) s_code[i] = code[i];
+   if (tid == 0)
+      s_code[meta.y] = make_uint2(meta_kind(meta) == kKindGeneric ? kGenericEnd : (uint32_t)M_END, 0u);
 }
 
 // ---- generic stack interpreter ----------------------------------------------
@@ -260,14 +270,31 @@ __device__ __forceinline__ void stager_init(uint64_t* bar) {
    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 }
 
+// Bounded wait for the current phase of the staging mbarrier (this thread's view).
+__device__ __forceinline__ bool wait_phase(const Stager& st) {
+   uint32_t done = 0;
+   for (int it = 0; it < kStageWaitLimit && !done; ++it) {
+      asm volatile(
+          "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+          : "=r"(done)
+          : "r"(smem_addr(st.bar)), "r"(st.phase)
+          : "memory");
+   }
+   return done != 0;
+}
+
 // Stage the records [base, base + T) of the program's staged columns (tile
 // rows s .. s+k-1, from the code header) and of the target column (row s+k),
 // and prefetch into L2 the same records of the columns it reads directly.
 // When the tile starts on a 16-byte boundary (always, except DP over a lane
 // count that is not a multiple of 4) one thread copies each column's segment
 // with cp.async.bulk (TMA) and every thread waits on the mbarrier; otherwise
-// the threads copy with 16-byte loads.  All threads call it.
-__device__ __forceinline__ void stage_tile(const float* data, int ncol, int ld, const uint2* s_code,
+// the threads copy with 16-byte loads.  All threads call it, and it returns
+// with the CTA synchronised (the tile visible to every thread).  Returns false,
+// the same in every thread, when the bulk copies did not complete within the
+// wait limit (kStatusStageTimeout is recorded): the CTA must stop staging and
+// end its work.
+__device__ __forceinline__ bool stage_tile(const float* data, int ncol, int ld, const uint2* s_code,
                                            float* s_tile, int base, int T, int tid, int P, Stager& st,
                                            int* status) {
    const uint2 hdr = s_code[0];
@@ -305,17 +332,18 @@ __device__ __forceinline__ void stage_tile(const float* data, int ncol, int ld, 
                 : "memory");
          }
       }
-      uint32_t done = 0;
-      for (int it = 0; it < kStageWaitLimit && !done; ++it) {
-         asm volatile(
-             "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
-             : "=r"(done)
-             : "r"(smem_addr(st.bar)), "r"(st.phase)
-             : "memory");
+      if (__syncthreads_and(wait_phase(st) ? 1 : 0)) {
+         st.phase ^= 1u;
+         return true;
       }
-      if (!done && tid == 0) atomicOr(status, kStatusStageTimeout);
-      st.phase ^= 1u;
-      return;
+      // The wait ran out: the phase of the mbarrier is no longer known, so
+      // this CTA stages nothing more.  Record it, give the copies in flight
+      // one more bounded wait (they target this CTA's shared memory), and
+      // let the caller end the CTA's work.
+      if (tid == 0) atomicOr(status, kStatusStageTimeout);
+      wait_phase(st);
+      __syncthreads();
+      return false;
    }
    for (int j = 0; j <= k; ++j) {
       const uint2 pair = s_code[1 + (j >> 1)];
@@ -327,12 +355,8 @@ __device__ __forceinline__ void stage_tile(const float* data, int ncol, int ld, 
          for (int q = 0; q < 4; ++q) dst[t + q] = (base + t + q < ld) ? __ldg(src + t + q) : 0.0f;
       }
    }
-}
-
-__device__ __forceinline__ unsigned long long fitness_key(float f, int prog) {
-   uint32_t u = __float_as_uint(f);
-   u = (u & 0x80000000u) ? ~u : (u | 0x80000000u);
-   return ((unsigned long long)u << 32) | (unsigned long long)(0xFFFFFFFFu - (uint32_t)prog);
+   __syncthreads();
+   return true;
 }
 
 __device__ __forceinline__ float reduce1(int reduce_max, float acc, float e, float fnlin) {
@@ -398,18 +422,22 @@ struct Job {
    int size;
    const uint2* code;          // in global memory
    int rows_cap;               // tile rows of this pass (lane accumulators follow them)
+   int alpha_free;             // the best index compares error/nlin without alpha*size
 };
 
 // Fitness of one program (valid in thread 0), in exactly the reference
-// strategy's accumulation order.  All threads of the CTA call it; it starts
-// and ends with the CTA synchronised.  s_code/s_tile: shared memory; the rows
+// strategy's accumulation order; `sel` (thread 0) receives the value the
+// best-index rule compares: the fitness, or error/nlin without alpha*size.
+// `abort` becomes true (in every thread) when a tile could not be staged;
+// the CTA must then take no more work.  All threads of the CTA call it; it
+// starts and ends with the CTA synchronised.  s_code/s_tile: shared memory; the rows
 // region holds job.rows_cap rows of T = P*R floats (slots, staged columns,
 // target; row 0 is reused for the tile's errors once the program has run),
 // then, unless the lane == tile-position path applies, lanes floats of lane
 // accumulators and lanes bytes of lane-finished flags.
 template <int MATH, int R, int OPSET, int D>
 __device__ float evaluate_program(const Job& j, uint2* s_code, float* s_tile, int* status, int tid,
-                                  int P, Stager& st) {
+                                  int P, Stager& st, float& sel, bool& abort) {
    const int T = P * R;
    const int L = j.lanes;
    const bool aligned = j.strategy == PPI_STRATEGY_PDP && L == T;
@@ -423,6 +451,7 @@ __device__ float evaluate_program(const Job& j, uint2* s_code, float* s_tile, in
    const int Teff = dp ? L * (T / L) : T;
    const float fnlin = (float)j.nlin;
    float fit = FLT_MAX;
+   sel = FLT_MAX;
    if (kind == kKindInvalid || kind == kKindUnsupported) {
       // size 0 (sizes outside [1, max_size] are treated as 0)
       if (tid == 0) {
@@ -433,12 +462,13 @@ __device__ float evaluate_program(const Job& j, uint2* s_code, float* s_tile, in
             const int G = (j.nlin + L - 1) / L;
             for (int g = 0; g < G; ++g) sum = reduce1(j.reduce_max, sum, FLT_MAX, fnlin);
             fit = nonfinite(sum) ? FLT_MAX : sum / fnlin;
+            sel = fit;
          }
       }
       __syncthreads();
       return fit;
    }
-   for (int i = tid; i < j.meta.y; i += P) s_code[i] = j.code[i];
+   load_code(s_code, j.code, j.meta, tid, P);
    if (!aligned)
       for (int l = tid; l < L; l += P) { s_acc[l] = 0.0f; s_done[l] = 0; }
    const uint2 hdr = j.code[0];
@@ -452,12 +482,17 @@ __device__ float evaluate_program(const Job& j, uint2* s_code, float* s_tile, in
    bool ddone = false;
    for (int base = 0; base < j.nlin; base += Teff) {
       __syncthreads();
-      stage_tile(j.data, j.ncol, j.ld, s_code, s_tile, base, T, tid, P, st, status);
-      __syncthreads();
+      if (!stage_tile(j.data, j.ncol, j.ld, s_code, s_tile, base, T, tid, P, st, status)) {
+         // the tile never arrived (status recorded): no fitness for this
+         // program, and the caller ends the CTA's work
+         abort = true;
+         fit = sel = __uint_as_float(0x7fc00000u);
+         return fit;
+      }
       float v[R];
       if (kind != kKindGeneric) {
          const Direct g{j.data + base, j.ld, j.ld - base, (base & 3) == 0};
-         run_fast<MATH, R, OPSET, D>(prog, s_tile + tid * 4, T, P, tid, g, v, j.prot);
+         run_fast<MATH, R, OPSET, D>(prog, s_tile + tid * 4, T, P, tid, g, v, j.prot, status);
       } else {
          float tmp[R];
          run_generic<MATH, R>(prog, j.data, j.ld, base, P, tid, tmp, j.prot);
@@ -526,7 +561,10 @@ __device__ float evaluate_program(const Job& j, uint2* s_code, float* s_tile, in
    }
    __syncthreads();
    if (dp) {
-      if (tid == 0) fit = nonfinite(dsum) ? FLT_MAX : dsum / fnlin + j.alpha * (float)j.size;
+      if (tid == 0) {
+         fit = nonfinite(dsum) ? FLT_MAX : dsum / fnlin + j.alpha * (float)j.size;
+         sel = fit;
+      }
    } else {
       if (aligned) {
          __syncthreads();   // every thread is done with the rows region
@@ -539,6 +577,7 @@ __device__ float evaluate_program(const Job& j, uint2* s_code, float* s_tile, in
          const float pe = s_acc[0];
          const float vv = nonfinite(pe) ? FLT_MAX : pe / fnlin;
          fit = vv + j.alpha * (float)j.size;
+         sel = j.alpha_free ? vv : fit;
       }
    }
    __syncthreads();
@@ -568,6 +607,7 @@ __global__ void __launch_bounds__(128, min_ctas_per_sm(MATH)) eval_kernel(const 
    j.strategy = a.strategy; j.lanes = a.lanes; j.ef = a.ef; j.reduce_max = a.reduce_max;
    j.prot = a.prot; j.cost = a.cost; j.cost_n = a.cost_n; j.alpha = a.alpha;
    j.rows_cap = a.rows;
+   j.alpha_free = a.best.alpha_free;
    unsigned* queue = a.wide_pass ? &a.stats->wide_queue : &a.stats->queue;
    const int limit = a.wide_pass ? (int)a.stats->wide : a.n;
    for (;;) {
@@ -583,11 +623,14 @@ __global__ void __launch_bounds__(128, min_ctas_per_sm(MATH)) eval_kernel(const 
       }
       j.size = a.size[prog];
       j.code = a.code + (size_t)prog * a.code_stride;
-      const float fit = evaluate_program<MATH, R, OPSET, D>(j, s_code, s_tile, a.status, tid, P, st);
+      float sel;
+      bool abort = false;
+      const float fit = evaluate_program<MATH, R, OPSET, D>(j, s_code, s_tile, a.status, tid, P, st, sel, abort);
       if (tid == 0) {
          a.fitness[prog] = fit;
-         atomicMin(a.best_key, fitness_key(fit, prog));
+         atomicMin(a.best_key, best_key(sel, best_tie(a.best, prog)));
       }
+      if (abort) break;   // staging failed: this CTA takes no more work
    }
    if (a.final_pass && tid == 0) {
       __threadfence();
@@ -595,7 +638,7 @@ __global__ void __launch_bounds__(128, min_ctas_per_sm(MATH)) eval_kernel(const 
       if (done == gridDim.x - 1) {
          __threadfence();
          const unsigned long long k = *reinterpret_cast<volatile unsigned long long*>(a.best_key);
-         a.best_index[0] = (int32_t)(0xFFFFFFFFu - (uint32_t)(k & 0xFFFFFFFFull));
+         a.best_index[0] = (int32_t)best_from_tie(a.best, (uint32_t)(k & 0xFFFFFFFFull));
       }
    }
 }
@@ -634,16 +677,23 @@ __global__ void __launch_bounds__(128, min_ctas_per_sm(MATH)) eval_batch_kernel(
       j.size = a.size[g];
       j.code = a.code + (size_t)g * a.code_stride;
       j.rows_cap = a.rows;
-      const float fit = evaluate_program<MATH, R, OPSET, D>(j, s_code, s_tile, a.status, tid, P, st);
+      j.alpha_free = pd.best.alpha_free;
+      float sel;
+      bool abort = false;
+      const float fit = evaluate_program<MATH, R, OPSET, D>(j, s_code, s_tile, a.status, tid, P, st, sel, abort);
+      if (abort) {   // staging failed: this CTA takes no more work
+         if (tid == 0) a.fitness[g] = fit;
+         break;
+      }
       if (tid == 0) {
          const int local = g - pd.prog_begin;
          a.fitness[g] = fit;
-         atomicMin(&a.pop_key[p], fitness_key(fit, local));
+         atomicMin(&a.pop_key[p], best_key(sel, best_tie(pd.best, local)));
          __threadfence();
          if (atomicAdd(&a.pop_done[p], 1u) == (unsigned)pd.n - 1) {
             __threadfence();
             const unsigned long long k = *reinterpret_cast<volatile unsigned long long*>(&a.pop_key[p]);
-            a.best_index[p] = (int32_t)(0xFFFFFFFFu - (uint32_t)(k & 0xFFFFFFFFull));
+            a.best_index[p] = (int32_t)best_from_tie(pd.best, (uint32_t)(k & 0xFFFFFFFFull));
          }
       }
    }
@@ -654,7 +704,6 @@ template <int MATH, int R, int OPSET>
 __global__ void __launch_bounds__(128, 4) predict_kernel(const PredictArgs a) {
    extern __shared__ __align__(16) unsigned char smem_raw[];
    __shared__ __align__(8) uint64_t s_bar;
-   __shared__ int s_status_unused;
    if (threadIdx.x == 0) stager_init(&s_bar);
    __syncthreads();
    Stager st{&s_bar, 0u};
@@ -662,20 +711,19 @@ __global__ void __launch_bounds__(128, 4) predict_kernel(const PredictArgs a) {
    const int2 m = a.meta[0];
    uint2* s_code = reinterpret_cast<uint2*>(smem_raw);
    float* s_tile = reinterpret_cast<float*>(smem_raw + code_bytes(m.y));
-   for (int i = tid; i < m.y; i += P) s_code[i] = a.code[i];
+   load_code(s_code, a.code, m, tid, P);
    const int kind = meta_kind(m);
    const bool runs = kind == kKindFast || kind == kKindWide || kind == kKindGeneric;
    const uint2 hdr = runs ? a.code[0] : make_uint2(0u, 0u);
    const uint2* prog = s_code + (runs ? code_header((int)hdr.x + (int)(hdr.y >> 16)) : 0);
    for (int base = blockIdx.x * T; base < a.nlin; base += gridDim.x * T) {
       __syncthreads();
-      if (runs)
-         stage_tile(a.data, a.ncol, a.ld, s_code, s_tile, base, T, tid, P, st, &s_status_unused);
-      __syncthreads();
+      if (runs && !stage_tile(a.data, a.ncol, a.ld, s_code, s_tile, base, T, tid, P, st, a.status))
+         break;   // the tile never arrived (status recorded): this CTA stops
       float v[R];
       if (kind == kKindFast || kind == kKindWide) {
          const Direct g{a.data + base, a.ld, a.ld - base, (base & 3) == 0};
-         run_fast<MATH, R, OPSET, 1>(prog, s_tile + tid * 4, T, P, tid, g, v, a.prot);
+         run_fast<MATH, R, OPSET, 1>(prog, s_tile + tid * 4, T, P, tid, g, v, a.prot, a.status);
       } else if (kind == kKindGeneric) {
          float tmp[R];
          run_generic<MATH, R>(prog, a.data, a.ld, base, P, tid, tmp, a.prot);

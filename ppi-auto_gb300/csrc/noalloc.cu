@@ -23,9 +23,13 @@
 // The translator rewrites everything the evaluator reads and resets the
 // counters, arg-min key and status word before use.  Calls whose work overlaps
 // on the GPU (different streams, or different host threads) race on the array
-// and must be serialised by the caller.
+// and must be serialised by the caller.  The kernels' status word (a program
+// the generic interpreter cannot hold, a tile copy that timed out, an
+// instruction outside the kernel's opcode set) is copied to the caller's
+// d_status at the end of the call's work, when the caller gives one.
 #include <cstdio>
 #include <cmath>
+#include <cstring>
 #include <mutex>
 
 #include "ppi_internal.cuh"
@@ -35,10 +39,13 @@ namespace {
 
 constexpr size_t kNoAllocScratchBytes = (size_t)64 << 20;   // 64 MiB
 constexpr int kMaxDevices = 64;
+// Widest Symbol range of the dense lookup table (as ppi_gpu_create).
+constexpr int kMaxSymbolRange = 1 << 22;
 
 __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
 unsigned char* g_scratch_addr[kMaxDevices] = {};
+int g_sm_count[kMaxDevices] = {};
 std::mutex g_scratch_mutex;
 
 inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
@@ -55,7 +62,7 @@ __global__ void noalloc_lut_kernel(const ppi_symbol_entry* entries, int n, int l
    lut[i] = v;
 }
 
-ppi_status scratch_base(int device, unsigned char** base) {
+ppi_status scratch_base(int device, unsigned char** base, int* sm_count) {
    std::lock_guard<std::mutex> lock(g_scratch_mutex);
    if (!g_scratch_addr[device]) {
       void* p = nullptr;
@@ -63,10 +70,52 @@ ppi_status scratch_base(int device, unsigned char** base) {
          std::fprintf(stderr, "ppi_gpu_evaluate_noalloc: cudaGetSymbolAddress failed on device %d\n", device);
          return PPI_ERR_CUDA;
       }
+      int sms = 0;
+      if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess || sms < 1)
+         return PPI_ERR_CUDA;
       g_scratch_addr[device] = static_cast<unsigned char*>(p);
+      g_sm_count[device] = sms;
    }
    *base = g_scratch_addr[device];
+   *sm_count = g_sm_count[device];
    return PPI_OK;
+}
+
+// Launch geometry of recent configurations.  plan_geometry asks the runtime
+// for dozens of occupancies; a generation loop calls this entry point with the
+// same configuration every time, so the result is kept (a pure function of
+// the key) in a small table replaced round robin.
+struct GeoKey {
+   int device, strategy, lanes, math, opset, nlin, ncol, code_stride, n;
+};
+struct GeoEntry {
+   GeoKey key;
+   Geometry geo;
+   bool used;
+};
+constexpr int kGeoCacheEntries = 16;
+GeoEntry g_geo_cache[kGeoCacheEntries] = {};
+int g_geo_next = 0;
+std::mutex g_geo_mutex;
+
+const char* cached_geometry(const GeoKey& k, int sm_count, Geometry* out) {
+   {
+      std::lock_guard<std::mutex> lock(g_geo_mutex);
+      for (const GeoEntry& e : g_geo_cache)
+         if (e.used && std::memcmp(&e.key, &k, sizeof k) == 0) {
+            *out = e.geo;
+            return nullptr;
+         }
+   }
+   Geometry g;
+   if (const char* why = plan_geometry(k.strategy, k.lanes, k.math, k.opset, k.nlin, k.ncol,
+                                       k.code_stride, k.n, sm_count, &g))
+      return why;
+   std::lock_guard<std::mutex> lock(g_geo_mutex);
+   g_geo_cache[g_geo_next] = GeoEntry{k, g, true};
+   g_geo_next = (g_geo_next + 1) % kGeoCacheEntries;
+   *out = g;
+   return nullptr;
 }
 
 }  // namespace
@@ -79,29 +128,38 @@ extern "C" ppi_status ppi_gpu_evaluate_noalloc(const ppi_gpu_config* c, const fl
                                                const int32_t* d_phenotype, const float* d_ephemeral,
                                                const int32_t* d_size, int32_t n, float alpha,
                                                float* d_fitness, int32_t* d_best_index,
-                                               void* stream) {
+                                               int32_t* d_status, void* stream) {
    if (!c || !d_data || !d_phenotype || !d_ephemeral || !d_size || !d_fitness || !d_best_index)
       return PPI_ERR_INVALID_ARGUMENT;
    if (c->max_size < 1 || c->max_size > 65535 || c->strategy < 0 || c->strategy > 2 ||
        c->error_fn < 0 || c->error_fn > 3 || c->math < 0 || c->math > 2 || c->lanes > kMaxLanes ||
        c->n_symbols < 0 || (c->n_symbols > 0 && !c->symbols) || n < 1 || nlin < 1 || ncol < 1 || ncol > kMaxColumns ||
        ld < nlin || (ld & 3) != 0 || (reinterpret_cast<uintptr_t>(d_data) & 15) != 0 ||
-       c->device < 0 || c->device >= kMaxDevices)
+       c->device < 0 || c->device >= kMaxDevices ||
+       (c->best_rule != PPI_BEST_ACCELERATOR && c->best_rule != PPI_BEST_SEQUENTIAL))
       return PPI_ERR_INVALID_ARGUMENT;
    if (c->error_fn == PPI_EF_COST && (!c->cost || c->cost_n < 1 || c->cost_n > 4096))
       return PPI_ERR_INVALID_ARGUMENT;
    for (int i = 0; i < c->n_symbols; ++i)
       if (c->symbols[i].op < 0 || c->symbols[i].op >= PPI_OP_COUNT) return PPI_ERR_INVALID_ARGUMENT;
-   if (cudaSetDevice(c->device) != cudaSuccess) return PPI_ERR_CUDA;
    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
 
-   // Symbol range of the table.
+   // Every size check comes before the first CUDA call.  Symbol range of the table, in 64 bits: a range wider than the dense
+   // table allows is rejected before any offset is derived from it.
    int mn = 0, mx = -1;
    for (int i = 0; i < c->n_symbols; ++i) {
       if (i == 0 || c->symbols[i].symbol < mn) mn = c->symbols[i].symbol;
       if (i == 0 || c->symbols[i].symbol > mx) mx = c->symbols[i].symbol;
    }
-   const int lut_len = c->n_symbols > 0 ? mx - mn + 1 : 0;
+   const long long range = c->n_symbols > 0 ? (long long)mx - (long long)mn + 1 : 0;
+   if (range < 0 || range > kMaxSymbolRange) {
+      std::fprintf(stderr,
+                   "ppi_gpu_evaluate_noalloc: the symbol table spans %lld values; at most %d are "
+                   "supported\n",
+                   range, kMaxSymbolRange);
+      return PPI_ERR_UNSUPPORTED;
+   }
+   const int lut_len = (int)range;
 
    // Scratch layout and its size limit.
    const int code_stride = 2 * c->max_size + 2;
@@ -115,7 +173,7 @@ extern "C" ppi_status ppi_gpu_evaluate_noalloc(const ppi_gpu_config* c, const fl
    const size_t off_work = align256(off_code + (size_t)n * code_stride * sizeof(uint2));
    const size_t off_wide = align256(off_work + (size_t)n * 2 * c->max_size * sizeof(uint2));
    const size_t total = align256(off_wide + (size_t)n * sizeof(int));
-   if (total > kNoAllocScratchBytes || lut_len > (1 << 22)) {
+   if (total > kNoAllocScratchBytes) {
       std::fprintf(stderr,
                    "ppi_gpu_evaluate_noalloc: %d programs of max_size %d need %zu bytes of scratch; "
                    "the fixed scratch holds %zu bytes (evaluate the population in smaller batches)\n",
@@ -123,19 +181,18 @@ extern "C" ppi_status ppi_gpu_evaluate_noalloc(const ppi_gpu_config* c, const fl
       return PPI_ERR_UNSUPPORTED;
    }
 
-   // Geometry: the lane rule and block choice of ppi_gpu_set_dataset.
+   if (cudaSetDevice(c->device) != cudaSuccess) return PPI_ERR_CUDA;
+   unsigned char* base = nullptr;
    int sm_count = 0;
-   if (cudaDeviceGetAttribute(&sm_count, cudaDevAttrMultiProcessorCount, c->device) != cudaSuccess)
-      return PPI_ERR_CUDA;
+   ppi_status st = scratch_base(c->device, &base, &sm_count);
+   if (st != PPI_OK) return st;
+
+   // Geometry: the lane rule and block choice of ppi_gpu_set_dataset.
    Geometry g;
    const int L = resolve_lanes(c->strategy, c->lanes, nlin, sm_count);
-   if (plan_geometry(c->strategy, L, c->math, opset_for(c->symbols, c->n_symbols), nlin, ncol,
-                     code_stride, n, sm_count, &g))
-      return PPI_ERR_UNSUPPORTED;
-
-   unsigned char* base = nullptr;
-   ppi_status st = scratch_base(c->device, &base);
-   if (st != PPI_OK) return st;
+   const GeoKey gk{c->device, c->strategy, L, c->math, opset_for(c->symbols, c->n_symbols),
+                   nlin, ncol, code_stride, n};
+   if (cached_geometry(gk, sm_count, &g)) return PPI_ERR_UNSUPPORTED;
    auto* key = reinterpret_cast<unsigned long long*>(base);
    auto* status = reinterpret_cast<int*>(base + 8);
    auto* stats = reinterpret_cast<DevStats*>(base + off_stats);
@@ -172,6 +229,9 @@ extern "C" ppi_status ppi_gpu_evaluate_noalloc(const ppi_gpu_config* c, const fl
    e.cost = cost; e.cost_n = c->cost_n; e.strategy = c->strategy; e.lanes = g.lanes; e.fitness = d_fitness;
    e.best_key = key; e.stats = stats; e.best_index = d_best_index; e.status = status;
    e.wide_list = wide;
+   if (best_geometry(c->best_rule, resolve_best_group(c->best_rule, c->best_group, n, sm_count),
+                     c->strategy, n, &e.best))
+      return PPI_ERR_UNSUPPORTED;
    if (cudaMemsetAsync(stats, 0, sizeof(DevStats), s) != cudaSuccess) return PPI_ERR_CUDA;
    if (launch_translate(c->math, t, s) != cudaSuccess) return PPI_ERR_CUDA;
    e.rows = g.rows; e.wide_pass = 0; e.final_pass = g.wide ? 0 : 1;
@@ -181,5 +241,8 @@ extern "C" ppi_status ppi_gpu_evaluate_noalloc(const ppi_gpu_config* c, const fl
       if (launch_evaluate(c->math, g.opset, g.wide_kernel, e, g.block, g.grid_wide, g.smem_wide, s) != cudaSuccess)
          return PPI_ERR_CUDA;
    }
+   // the kernels' status bits, for the caller to read once the stream is done
+   if (d_status && cudaMemcpyAsync(d_status, status, sizeof(int32_t), cudaMemcpyDeviceToDevice, s) != cudaSuccess)
+      return PPI_ERR_CUDA;
    return PPI_OK;
 }

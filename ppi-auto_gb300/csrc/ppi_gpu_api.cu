@@ -34,6 +34,7 @@ struct ppi_gpu {
    bool have_data = false;
    int lanes = 1;
    int opset = kOpsetFull;
+   int best_group = 1;         // work-group size of the best-index rule
    Geometry geo;
    // per-generation buffers (capacity population_size)
    int32_t* d_ph = nullptr;
@@ -67,6 +68,7 @@ struct ppi_gpu {
    size_t frames_cap = 0;
    float last_ms = 0.0f;
    int last_launches = 0;
+   int last_n = 0;                 // programs of the last translation
    // constant adjoint (allocated on first use)
    uint2* d_adj_code = nullptr;
    int2* d_adj_meta = nullptr;
@@ -130,6 +132,18 @@ ppi_status plan(ppi_gpu* h) {
    return PPI_OK;
 }
 
+// Status word of the last kernels, as a ppi_status and message.
+ppi_status device_status(ppi_gpu* h, int bits) {
+   if (bits & kStatusStageTimeout)
+      return fail(h, PPI_ERR_DEVICE_STATUS, "a tile copy did not complete (bounded wait expired)");
+   if (bits & kStatusBadInstruction)
+      return fail(h, PPI_ERR_DEVICE_STATUS, "a kernel met an instruction outside its opcode set");
+   if (bits & kStatusUnsupportedProgram)
+      return fail(h, PPI_ERR_UNSUPPORTED,
+                  "a malformed program needs a deeper stack than the generic interpreter's");
+   return PPI_OK;
+}
+
 ppi_status check_ready(ppi_gpu* h, int n) {
    if (!h) return PPI_ERR_INVALID_ARGUMENT;
    if (!h->have_data) return fail(h, PPI_ERR_NOT_READY, "no dataset: call ppi_gpu_set_dataset first");
@@ -158,9 +172,12 @@ ppi_status enqueue(ppi_gpu* h, const int32_t* d_ph, const float* d_eph, const in
    e.strategy = h->cfg.strategy; e.lanes = h->lanes; e.fitness = d_fit; e.best_key = h->d_key;
    e.stats = h->d_stats; e.best_index = d_best; e.status = h->d_status;
    e.wide_list = h->d_wide;
+   if (const char* why = best_geometry(h->cfg.best_rule, h->best_group, h->cfg.strategy, n, &e.best))
+      return fail(h, PPI_ERR_UNSUPPORTED, why);
    PPI_CUDA(h, cudaEventRecord(h->ev0, s));
    PPI_CUDA(h, cudaMemsetAsync(h->d_stats, 0, sizeof(DevStats), s));
    PPI_CUDA(h, launch_translate(h->cfg.math, t, s));
+   h->last_n = n;
    PPI_CUDA(h, cudaEventRecord(h->evm, s));
    e.rows = g.rows; e.wide_pass = 0; e.final_pass = g.wide ? 0 : 1;
    PPI_CUDA(h, launch_evaluate(h->cfg.math, g.opset, 0, e, g.block, std::min(g.grid, n), g.smem, s));
@@ -179,7 +196,7 @@ ppi_status enqueue(ppi_gpu* h, const int32_t* d_ph, const float* d_eph, const in
 
 extern "C" {
 
-const char* ppi_gpu_version(void) { return "ppi_gpu 1 sm_103a"; }
+const char* ppi_gpu_version(void) { return "ppi_gpu 2 sm_103a"; }
 
 const char* ppi_gpu_last_error(const ppi_gpu* h) { return h ? h->err.c_str() : "null handle"; }
 
@@ -189,7 +206,8 @@ ppi_status ppi_gpu_create(const ppi_gpu_config* c, ppi_gpu** out) {
    if (c->max_size < 1 || c->max_size > 65535 || c->population_size < 1 ||
        c->strategy < 0 || c->strategy > 2 || c->error_fn < 0 || c->error_fn > 3 || c->math < 0 ||
        c->math > 2 || c->lanes > kMaxLanes || c->n_symbols < 0 ||
-       (c->n_symbols > 0 && !c->symbols))
+       (c->n_symbols > 0 && !c->symbols) ||
+       (c->best_rule != PPI_BEST_ACCELERATOR && c->best_rule != PPI_BEST_SEQUENTIAL))
       return PPI_ERR_INVALID_ARGUMENT;
    if (c->error_fn == PPI_EF_COST && (!c->cost || c->cost_n < 1 || c->cost_n > 4096))
       return PPI_ERR_INVALID_ARGUMENT;
@@ -204,6 +222,7 @@ ppi_status ppi_gpu_create(const ppi_gpu_config* c, ppi_gpu** out) {
    if (c->device < 0 || c->device >= ndev) return bail(PPI_ERR_INVALID_ARGUMENT);
    if (cudaSetDevice(c->device) != cudaSuccess) return bail(PPI_ERR_CUDA);
    cudaDeviceGetAttribute(&h->sm_count, cudaDevAttrMultiProcessorCount, c->device);
+   h->best_group = resolve_best_group(c->best_rule, c->best_group, c->population_size, h->sm_count);
    if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess ||
        cudaEventCreate(&h->ev0) != cudaSuccess || cudaEventCreate(&h->ev1) != cudaSuccess || cudaEventCreate(&h->evm) != cudaSuccess)
       return bail(PPI_ERR_CUDA);
@@ -332,12 +351,7 @@ ppi_status ppi_gpu_evaluate_wait(ppi_gpu* h) {
    std::memcpy(h->out_fit, h->h_fit, (size_t)h->pending_n * sizeof(float));
    if (h->out_best) *h->out_best = *h->h_best;
    cudaEventElapsedTime(&h->last_ms, h->ev0, h->ev1);
-   if (*h->h_status & kStatusStageTimeout)
-      return fail(h, PPI_ERR_DEVICE_STATUS, "a tile copy did not complete (bounded wait expired)");
-   if (*h->h_status & kStatusUnsupportedProgram)
-      return fail(h, PPI_ERR_UNSUPPORTED,
-                  "a malformed program needs a deeper stack than the generic interpreter's");
-   return PPI_OK;
+   return device_status(h, *h->h_status);
 }
 
 ppi_status ppi_gpu_evaluate(ppi_gpu* h, const int32_t* ph, const float* eph, const int32_t* size,
@@ -391,6 +405,7 @@ ppi_status ppi_gpu_predict(ppi_gpu* h, const int32_t* ph, const float* eph, int3
    PredictArgs p{};
    p.data = h->d_data; p.nlin = h->nlin; p.ncol = h->ncol; p.ld = h->ld;
    p.code = h->d_code; p.meta = h->d_meta; p.prot = h->cfg.protected_fns ? 1 : 0; p.out = h->d_pred;
+   p.status = h->d_status;   // zeroed by the translator
    const int tiles = (h->nlin + P * R - 1) / (P * R);
    const int grid = std::max(1, std::min(tiles, 4 * h->sm_count));
    PPI_CUDA(h, cudaEventRecord(h->ev0, h->stream));
@@ -399,10 +414,12 @@ ppi_status ppi_gpu_predict(ppi_gpu* h, const int32_t* ph, const float* eph, int3
    PPI_CUDA(h, launch_predict(h->cfg.math, h->opset, p, P, grid, smem, h->stream));
    PPI_CUDA(h, cudaEventRecord(h->ev1, h->stream));
    PPI_CUDA(h, cudaMemcpyAsync(out, h->d_pred, (size_t)h->nlin * 4, cudaMemcpyDeviceToHost, h->stream));
+   PPI_CUDA(h, cudaMemcpyAsync(h->h_status, h->d_status, 4, cudaMemcpyDeviceToHost, h->stream));
    PPI_CUDA(h, cudaStreamSynchronize(h->stream));
    cudaEventElapsedTime(&h->last_ms, h->ev0, h->ev1);
    h->last_launches = 2;
-   return PPI_OK;
+   // an unsupported program predicts NaN on every record, as before
+   return device_status(h, *h->h_status & (kStatusStageTimeout | kStatusBadInstruction));
 }
 
 // Adjoint launch planning: occupancy levels per R (CTAs per SM, 0 = the
@@ -551,9 +568,7 @@ ppi_status ppi_gpu_constant_gradient(ppi_gpu* h, const int32_t* ph, const float*
    PPI_CUDA(h, cudaMemcpyAsync(h->h_status, h->d_status, sizeof(int), cudaMemcpyDeviceToHost, st));
    PPI_CUDA(h, cudaStreamSynchronize(st));
    cudaEventElapsedTime(&h->last_ms, h->ev0, h->ev1);
-   if (*h->h_status & kStatusStageTimeout)
-      return fail(h, PPI_ERR_DEVICE_STATUS, "a tile copy did not complete (bounded wait expired)");
-   return PPI_OK;
+   return device_status(h, *h->h_status & (kStatusStageTimeout | kStatusBadInstruction));
 }
 
 ppi_status ppi_gpu_last_kernel_ms(ppi_gpu* h, float* ms) {
@@ -565,6 +580,22 @@ ppi_status ppi_gpu_last_kernel_ms(ppi_gpu* h, float* ms) {
 int32_t ppi_gpu_last_launch_count(const ppi_gpu* h) { return h ? h->last_launches : 0; }
 
 int32_t ppi_gpu_lanes(const ppi_gpu* h) { return (h && h->have_data) ? h->lanes : 0; }
+
+ppi_status ppi_gpu_translation(ppi_gpu* h, int32_t n, uint32_t* code, int32_t* meta,
+                               int32_t* code_stride, int32_t* opset) {
+   if (!h || !code_stride || !opset) return PPI_ERR_INVALID_ARGUMENT;
+   *code_stride = h->code_stride;
+   *opset = h->opset;
+   if (!code && !meta) return PPI_OK;
+   if (n < 0 || n > h->last_n) return fail(h, PPI_ERR_INVALID_ARGUMENT, "n exceeds the last translation");
+   if (n == 0) return PPI_OK;
+   PPI_CUDA(h, cudaSetDevice(h->device));
+   PPI_CUDA(h, cudaDeviceSynchronize());
+   if (code)
+      PPI_CUDA(h, cudaMemcpy(code, h->d_code, (size_t)n * h->code_stride * sizeof(uint2), cudaMemcpyDeviceToHost));
+   if (meta) PPI_CUDA(h, cudaMemcpy(meta, h->d_meta, (size_t)n * sizeof(int2), cudaMemcpyDeviceToHost));
+   return PPI_OK;
+}
 
 ppi_status ppi_gpu_last_stage_ms(ppi_gpu* h, float* translate_ms, float* evaluate_ms) {
    if (!h || !translate_ms || !evaluate_ms) return PPI_ERR_INVALID_ARGUMENT;
@@ -680,11 +711,7 @@ ppi_status ppi_gpu_decode_evaluate(ppi_gpu* h, const uint8_t* genomes, int32_t n
    std::memcpy(fitness, h->h_fit, (size_t)n * sizeof(float));
    if (best_index) *best_index = *h->h_best;
    cudaEventElapsedTime(&h->last_ms, h->ev0, h->ev1);
-   if (*h->h_status & kStatusStageTimeout)
-      return fail(h, PPI_ERR_DEVICE_STATUS, "a tile copy did not complete (bounded wait expired)");
-   if (*h->h_status & kStatusUnsupportedProgram)
-      return fail(h, PPI_ERR_UNSUPPORTED, "a program needs a deeper stack than supported");
-   return PPI_OK;
+   return device_status(h, *h->h_status);
 }
 
 }  // extern "C"

@@ -63,8 +63,10 @@ struct DevStats {
    unsigned wide_queue;      // work queue of the wide pass
 };
 
-// Status bits reported by the kernels.
-enum : int { kStatusUnsupportedProgram = 1, kStatusStageTimeout = 2 };
+// Status bits reported by the kernels: a program the generic interpreter
+// cannot hold; a tile copy that did not complete within the bounded wait (the
+// CTA stopped); an instruction outside the running kernel's opcode set.
+enum : int { kStatusUnsupportedProgram = 1, kStatusStageTimeout = 2, kStatusBadInstruction = 4 };
 
 // Accumulator-machine instructions.  Each is a uint2: .x = instruction id
 // below, .y = immediate: float bits of a constant, or a row index.
@@ -282,6 +284,68 @@ __device__ __forceinline__ float apply_error_t(float x, float y, const float* co
 }
 
 // ---------------------------------------------------------------------------
+// Best index.  The reference's accelerator picks it in two steps: the
+// best_individual kernel (accelerator.cl:271-313) reduces each work-group of
+// `group` programs by a strided tree that replaces the left value only when
+// it is strictly greater, and util::PickNBest on the host takes the smallest
+// group winner, ties to the largest group (accelerator.cc:871-880).  Two
+// tied programs of one group meet at the lowest bit where their positions in
+// the group differ, and the one with a 0 there is on the left and wins; so
+// the tree's winner is the smallest value, then the smallest bit-reversed
+// position.  The whole rule is therefore one lexicographic order -- value,
+// then largest group, then smallest bit-reversed position -- and one 64-bit
+// atomicMin per program implements it: the orderable value bits on top, the
+// tie field below.  The sequential rule (ties to the largest index,
+// sequential.cc:203) is the same order with groups of one program.
+struct BestGeo {
+   int group;                  // programs per work-group (1: sequential rule)
+   int bits;                   // ceil(log2(group)): width of a position
+   int groups;                 // ceil(n / group)
+   int alpha_free;             // compare error/nlin without alpha*size (PP, PDP)
+};
+
+__host__ __device__ __forceinline__ uint32_t reverse_bits(uint32_t v, int bits) {
+#ifdef __CUDA_ARCH__
+   return bits > 0 ? (__brev(v) >> (32 - bits)) : 0u;
+#else
+   uint32_t r = 0;
+   for (int b = 0; b < bits; ++b) r |= ((v >> b) & 1u) << (bits - 1 - b);
+   return r;
+#endif
+}
+
+// Tie field of program `prog`: smaller is better.
+__host__ __device__ __forceinline__ uint32_t best_tie(const BestGeo& b, int prog) {
+   const uint32_t g = (uint32_t)(prog / b.group), lo = (uint32_t)(prog - (int)g * b.group);
+   return (((uint32_t)b.groups - 1u - g) << b.bits) | reverse_bits(lo, b.bits);
+}
+
+__host__ __device__ __forceinline__ int best_from_tie(const BestGeo& b, uint32_t tie) {
+   const uint32_t g = (uint32_t)b.groups - 1u - (b.bits < 32 ? (tie >> b.bits) : 0u);
+   const uint32_t lo = reverse_bits(tie & ((1u << b.bits) - 1u), b.bits);
+   return (int)(g * (uint32_t)b.group + lo);
+}
+
+// 64-bit arg-min key: float order on top (FLT_MAX sentinels included), tie below.
+__host__ __device__ __forceinline__ unsigned long long best_key(float f, uint32_t tie) {
+   uint32_t u;
+#ifdef __CUDA_ARCH__
+   u = __float_as_uint(f);
+#else
+   __builtin_memcpy(&u, &f, 4);
+#endif
+   u = (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+   return ((unsigned long long)u << 32) | (unsigned long long)tie;
+}
+
+// Work-group size of the reference's best_individual launch: config value,
+// else min(1024, ceil(population / compute units)) (accelerator.cc:289-294,
+// 348) on a device whose work-groups reach 1024 items.
+int resolve_best_group(int rule, int group, int population, int sm_count);
+// Geometry of the rule for n programs; nullptr, or why it cannot be encoded.
+const char* best_geometry(int rule, int group, int strategy, int n, BestGeo* out);
+
+// ---------------------------------------------------------------------------
 // One population of a batch (device memory).
 struct PopDesc {
    const float* data;          // column-major, column c at data + c * ld
@@ -291,6 +355,7 @@ struct PopDesc {
    float alpha;
    int prog_begin;             // first program of the population in the flat arrays
    int n;                      // programs
+   BestGeo best;               // the population's best-index rule
 };
 
 struct TranslateArgs {
@@ -341,6 +406,7 @@ struct EvalArgs {
    int wide_pass;              // 0: main pass (skips kKindWide), 1: programs of wide_list
    const int* wide_list;
    int final_pass;             // this pass writes the best index
+   BestGeo best;               // best-index rule
 };
 
 struct BatchArgs {
@@ -370,6 +436,7 @@ struct PredictArgs {
    const int2* meta;
    int prot;
    float* out;
+   int* status;                // kStatus* bits
 };
 
 // ---------------------------------------------------------------------------

@@ -43,7 +43,13 @@ class Config(C.Structure):
                 ("lanes", C.c_int32), ("error_fn", C.c_int32), ("reduce_max", C.c_int32),
                 ("protected_fns", C.c_int32), ("math", C.c_int32), ("cost", _fp),
                 ("cost_n", C.c_int32), ("symbols", C.POINTER(SymbolEntry)),
-                ("n_symbols", C.c_int32), ("device", C.c_int32)]
+                ("n_symbols", C.c_int32), ("device", C.c_int32), ("best_rule", C.c_int32),
+                ("best_group", C.c_int32)]
+
+
+# ppi_best_rule: "accelerator" = the index acc_interpret returns (best_individual
+# work-groups + PickNBest), "sequential" = the index seq_interpret returns.
+BEST_RULE = {"accelerator": 0, "sequential": 1}
 
 
 class BatchPopulation(C.Structure):
@@ -98,6 +104,8 @@ def load_library():
     L.ppi_gpu_last_launch_count.argtypes = [C.c_void_p]
     L.ppi_gpu_last_stage_ms.argtypes = [C.c_void_p, _fp, _fp]
     L.ppi_gpu_lanes.argtypes = [C.c_void_p]
+    L.ppi_gpu_translation.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_uint32), _ip, _ip, _ip]
+    L.ppi_gpu_kernel_arch.restype = C.c_int32
     L.ppi_gpu_constant_gradient.argtypes = [C.c_void_p, _ip, _fp, _ip, C.c_int32, _fp]
     L.ppi_batch_create.argtypes = [C.POINTER(Config), C.c_int32, C.POINTER(BatchPopulation),
                                    C.POINTER(C.c_void_p)]
@@ -136,7 +144,7 @@ class Evaluator:
 
     def __init__(self, symtab, max_size, population_size, strategy="PDP", lanes=0,
                  error_fn="abs", cost=None, reduce_max=False, protected=False, math="fast",
-                 device=0):
+                 device=0, best_rule="accelerator", best_group=0):
         L = load_library()
         sv, so, sl = symtab
         self._syms = (SymbolEntry * max(1, len(sv)))()
@@ -147,7 +155,7 @@ class Evaluator:
                      int(reduce_max), int(protected), MATH[math],
                      _f(self._cost) if self._cost is not None else None,
                      0 if self._cost is None else self._cost.shape[0], self._syms, len(sv),
-                     device)
+                     device, BEST_RULE[best_rule], int(best_group))
         self._config = cfg
         h = C.c_void_p()
         st = L.ppi_gpu_create(C.byref(cfg), C.byref(h))
@@ -261,6 +269,18 @@ class Evaluator:
         self._check(self._L.ppi_gpu_last_stage_ms(self._h, _f(t[0:1]), _f(t[1:2])))
         return float(t[0]), float(t[1])
 
+    def translation(self, n):
+        """The last evaluate call's bytecode: (code uint32 [n, stride, 2],
+        meta int32 [n, 2], opset) -- see ppi_gpu_translation."""
+        stride = np.zeros(1, np.int32)
+        opset = np.zeros(1, np.int32)
+        self._check(self._L.ppi_gpu_translation(self._h, 0, None, None, _i(stride), _i(opset)))
+        code = np.zeros((n, int(stride[0]), 2), np.uint32)
+        meta = np.zeros((n, 2), np.int32)
+        self._check(self._L.ppi_gpu_translation(self._h, n, code.ctypes.data_as(C.POINTER(C.c_uint32)),
+                                                _i(meta), _i(stride), _i(opset)))
+        return code, meta, int(opset[0])
+
     @property
     def lanes(self):
         return int(self._L.ppi_gpu_lanes(self._h))
@@ -276,13 +296,15 @@ class BatchEvaluator:
     error_fn, cost, reduce_max, protected.  Programs, fitness: all
     populations concatenated in order (rows of max_size)."""
 
-    def __init__(self, symtab, max_size, pops, math="fast", device=0):
+    def __init__(self, symtab, max_size, pops, math="fast", device=0, best_rule="accelerator",
+                 best_group=0):
         L = load_library()
         sv, so, sl = symtab
         self._syms = (SymbolEntry * max(1, len(sv)))()
         for k in range(len(sv)):
             self._syms[k] = SymbolEntry(int(sv[k]), int(so[k]), float(sl[k]))
-        cfg = Config(max_size, 1, 0, 0, 0, 0, 0, MATH[math], None, 0, self._syms, len(sv), device)
+        cfg = Config(max_size, 1, 0, 0, 0, 0, 0, MATH[math], None, 0, self._syms, len(sv), device,
+                     BEST_RULE[best_rule], int(best_group))
         self._keep = []
         arr = (BatchPopulation * len(pops))()
         for i, p in enumerate(pops):

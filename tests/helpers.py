@@ -63,6 +63,39 @@ def enum_values(text):
     return out
 
 
+def device_sm_count():
+    """Compute units the library's automatic best_individual group size uses."""
+    import torch
+    return torch.cuda.get_device_properties(0).multi_processor_count
+
+
+def auto_best_group(population):
+    """The reference's best_individual work-group size for a population on
+    this device: min(1024, ceil(population / compute units))
+    (src/interpreter/accelerator.cc:348)."""
+    cu = device_sm_count()
+    return max(1, min(1024, -(-int(population) // cu)))
+
+
+def expected_best(oracle_lib, o, ph, ep, sz, strategy, lanes, alpha, rule="accelerator",
+                  group=None, population=None):
+    """The best index the reference returns for these programs.
+
+    sequential: util::PickNBest over the alpha-included fitness
+    (sequential.cc:203).  accelerator: best_individual over work-groups of
+    `group` programs (default: the automatic size for `population`, itself
+    defaulting to the number of programs), then PickNBest over the group
+    winners, comparing error/nlin for PP/PDP and the alpha-included fitness for
+    DP (accelerator.cc:491,500,848-849,871-880)."""
+    fit = o.evaluate(ph, ep, sz, strategy, lanes, alpha)
+    if rule == "sequential":
+        return oracle_lib.best_index(fit)
+    vals = fit if strategy == "DP" else o.evaluate(ph, ep, sz, strategy, lanes, 0.0)
+    if group is None or group <= 0:
+        group = auto_best_group(population or len(sz))
+    return oracle_lib.best_index_accelerator(vals, group)
+
+
 def bits(a):
     return np.ascontiguousarray(a, np.float32).view(np.int32)
 
@@ -78,11 +111,12 @@ def assert_bitexact(a, b, what=""):
 
 
 def make_evaluator(d, strategy="PDP", lanes=0, math="parity", population=None, max_size=None,
-                   rows=None):
+                   rows=None, best_rule="accelerator", best_group=0):
     import ppi_gpu
     ev = ppi_gpu.Evaluator(d["symtab"], max_size or d["max_size"],
                            population or len(d["size"]), strategy, lanes, d["ef"],
-                           d["cost_or_none"], bool(d["reduce_max"]), bool(d["protected"]), math)
+                           d["cost_or_none"], bool(d["reduce_max"]), bool(d["protected"]), math,
+                           best_rule=best_rule, best_group=best_group)
     ev.set_dataset(d["rows"] if rows is None else rows)
     return ev
 

@@ -23,7 +23,8 @@ def test_adapter_compiles_with_generated_headers(tmp_path, opts):
 def test_adapter_compiles_against_ppi_headers(tmp_path):
     from oracle import pyoracle
     man = pyoracle.ref_manifest()
-    ref_interp = "/root/reference/src/interpreter"
+    from oracle.build_ref import reference_root
+    ref_interp = os.path.join(reference_root(), "src", "interpreter")
     if not man or not os.path.exists(os.path.join(ref_interp, "accelerator.h")):
         pytest.skip("reference tree not present")
     for name in ("cfg2", "iris", "random"):

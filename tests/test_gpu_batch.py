@@ -5,7 +5,7 @@ alone with the plain evaluator (and, in parity math, to the oracle)."""
 import numpy as np
 import pytest
 
-from helpers import ProgramGen, assert_bitexact, load_golden
+from helpers import ProgramGen, assert_bitexact, expected_best, load_golden
 
 pytestmark = pytest.mark.gpu
 
@@ -99,6 +99,10 @@ def test_batch_matches_plain_evaluations(gpu_lib, oracle_lib, math, flags):
                                         p.get("reduce_max", 0), p.get("protected", 0)).evaluate(
                     ph[sl], ep[sl], sz[sl], p.get("strategy", "PDP"), lanes, alpha[k])
                 assert_bitexact(fit[sl], ref, "oracle, population %d" % k)
+                o = oracle_lib.Oracle(p["rows"], d["symtab"], p["error_fn"], p.get("cost"),
+                                      p.get("reduce_max", 0), p.get("protected", 0))
+                assert best[k] == expected_best(oracle_lib, o, ph[sl], ep[sl], sz[sl],
+                                                p.get("strategy", "PDP"), lanes, alpha[k]), k
             begin += p["n"]
     block, grid, rows, tune = be.shape()
     assert block in (64, 128) and grid >= 1

@@ -8,8 +8,8 @@ relative tolerance."""
 import numpy as np
 import pytest
 
-from helpers import (Tables, assert_bitexact, golden_names, load_golden, make_evaluator,
-                     oracle_for)
+from helpers import (Tables, assert_bitexact, expected_best, golden_names, load_golden,
+                     make_evaluator, oracle_for)
 
 pytestmark = pytest.mark.gpu
 NAMES = golden_names()
@@ -22,10 +22,25 @@ FAST_RTOL = 1e-4
 @pytest.mark.parametrize("name", NAMES)
 def test_pp_parity_equals_sequential_reference(gpu_lib, name):
     d = load_golden(name)
-    ev = make_evaluator(d, "PP", 0, "parity")
+    ev = make_evaluator(d, "PP", 0, "parity", best_rule="sequential")
     f, best = ev.evaluate(d["phenotype"], d["ephemeral"], d["size"], float(d["alpha"]))
     assert_bitexact(f, d["seq_fitness"], name)
     assert best == d["seq_best"]
+
+
+# The fixtures' cl_<strategy>_<lanes>_best are the indices the reference's own
+# evaluate_* and best_individual kernels (work-groups of 16) and its host
+# PickNBest returned on these programs.
+CL_CASES = [("PP", 16), ("PDP", 64), ("PDP", 7), ("DP", 32), ("DP", 5)]
+
+
+@pytest.mark.parametrize("name", NAMES)
+@pytest.mark.parametrize("strat,lanes", CL_CASES)
+def test_best_index_equals_accelerator_reference(gpu_lib, name, strat, lanes):
+    d = load_golden(name)
+    ev = make_evaluator(d, strat, 0 if strat == "PP" else lanes, "parity", best_group=16)
+    _, best = ev.evaluate(d["phenotype"], d["ephemeral"], d["size"], float(d["alpha"]))
+    assert best == int(d["cl_%s_%d_best" % (strat, lanes)]), (name, strat, lanes)
 
 
 @pytest.mark.parametrize("name", NAMES)
@@ -38,7 +53,9 @@ def test_strategy_orders_bitexact(gpu_lib, oracle_lib, name, strat, lanes):
     ref = oracle_for(oracle_lib, d).evaluate(d["phenotype"], d["ephemeral"], d["size"], strat, L,
                                             float(d["alpha"]))
     assert_bitexact(f, ref, "%s %s%d" % (name, strat, lanes))
-    assert best == oracle_lib.best_index(ref)
+    o = oracle_for(oracle_lib, d)
+    assert best == expected_best(oracle_lib, o, d["phenotype"], d["ephemeral"], d["size"], strat, L,
+                                 float(d["alpha"]))
 
 
 @pytest.mark.parametrize("name", NAMES)

@@ -6,7 +6,8 @@ divide the records, one record, and tiny populations."""
 import numpy as np
 import pytest
 
-from helpers import ProgramGen, assert_bitexact, load_golden, make_evaluator, oracle_for
+from helpers import (ProgramGen, assert_bitexact, expected_best, load_golden, make_evaluator,
+                     oracle_for)
 
 pytestmark = pytest.mark.gpu
 
@@ -24,9 +25,10 @@ def _check(oracle_lib, d, rows, ph, ep, sz, strat, lanes, math="parity", alpha=1
     assert L == (1 if strat == "PP" else lanes if lanes > 0 and strat == "DP" else
                  min(lanes, len(rows)) if lanes > 0 else
                  min(len(rows), 1024) if strat == "PDP" else min(1024, -(-len(rows) // 152)))
-    ref = oracle_for(oracle_lib, d, rows=rows).evaluate(ph, ep, sz, strat, L, alpha)
+    o = oracle_for(oracle_lib, d, rows=rows)
+    ref = o.evaluate(ph, ep, sz, strat, L, alpha)
     assert_bitexact(f, ref, "%s%d" % (strat, lanes))
-    assert best == oracle_lib.best_index(ref)
+    assert best == expected_best(oracle_lib, o, ph, ep, sz, strat, L, alpha)
     return f
 
 
@@ -226,11 +228,13 @@ def test_wide_dataset_staged_and_direct_columns(gpu_lib, oracle_lib, strat, lane
     # occupancy-driven size (a population that fits one wave gets every row it
     # can use), so the wide programs take the direct-read path
     ev = make_evaluator(d, strat, lanes, "parity", population=20000, max_size=200, rows=rows)
-    ref = oracle_for(oracle_lib, d, rows=rows).evaluate(ph, ep, sz, strat, ev.lanes, 1e-6)
+    o = oracle_for(oracle_lib, d, rows=rows)
+    ref = o.evaluate(ph, ep, sz, strat, ev.lanes, 1e-6)
+    want = expected_best(oracle_lib, o, ph, ep, sz, strat, ev.lanes, 1e-6, population=20000)
     for rep in range(2):
         f, best = ev.evaluate(ph, ep, sz, 1e-6)
         assert_bitexact(f, ref, "%s%d rep %d" % (strat, lanes, rep))
-        assert best == oracle_lib.best_index(ref)
+        assert best == want
     pred = ev.predict(ph[-1], ep[-1], int(sz[-1]))
     assert_bitexact(pred, oracle_for(oracle_lib, d, rows=rows).predict(ph[-1], ep[-1], int(sz[-1])),
                     "predict")

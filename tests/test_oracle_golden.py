@@ -55,3 +55,29 @@ def test_opencl_strategies_bitexact(oracle_lib, name, strat, lanes):
 def test_best_index_ties_go_to_largest_index(oracle_lib):
     f = np.array([3, 1, 2, 1, 5, 1, 9], np.float32)
     assert oracle_lib.best_index(f) == 5
+
+
+@pytest.mark.parametrize("name", NAMES)
+@pytest.mark.parametrize("strat,lanes", [("PP", 16), ("PDP", 64), ("PDP", 7), ("DP", 32), ("DP", 5)])
+def test_accelerator_best_index_matches_reference_kernels(oracle_lib, name, strat, lanes):
+    """best_individual (work-groups of 16) + PickNBest over the alpha-free
+    values (PP, PDP) or the alpha-included fitness (DP), against the index the
+    reference's own kernels returned for the fixture."""
+    d = load_golden(name)
+    o = oracle_for(oracle_lib, d, float_math=True)
+    L = 1 if strat == "PP" else lanes
+    alpha = float(d["alpha"]) if strat == "DP" else 0.0
+    vals = o.evaluate(d["phenotype"], d["ephemeral"], d["size"], strat, L, alpha)
+    assert oracle_lib.best_index_accelerator(vals, 16) == int(d["cl_%s_%d_best" % (strat, lanes)])
+
+
+def test_accelerator_best_index_tree_order(oracle_lib):
+    """The strided tree keeps the left value on ties, so among equal values
+    the winner is not always the smallest index: with groups of 4, values
+    (5, 1, 1, 9) reduce as min(v0, v2) = v2 and min(v1, v3) = v1, then v2
+    (left) beats v1.  Across groups, ties go to the last group."""
+    v = np.array([5, 1, 1, 9], np.float32)
+    assert oracle_lib.best_index_accelerator(v, 4) == 2
+    v = np.array([2, 0, 3, 3, 0, 7, 7, 7], np.float32)
+    assert oracle_lib.best_index_accelerator(v, 4) == 4
+    assert oracle_lib.best_index_accelerator(v, 1) == oracle_lib.best_index(v) == 4

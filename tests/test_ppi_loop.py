@@ -11,8 +11,10 @@ import subprocess
 
 import pytest
 
-REF_SRC = "/root/reference/src"
-DATA = "/root/reference/problem/polynomial/data.csv"
+from oracle.build_ref import reference_root
+
+REF_SRC = os.path.join(reference_root(), "src")
+DATA = os.path.join(reference_root(), "problem", "polynomial", "data.csv")
 
 
 @pytest.fixture(scope="module")

@@ -20,7 +20,7 @@ def _entry(lib):
     f = lib.ppi_gpu_evaluate_noalloc
     f.argtypes = [C.POINTER(ppi_gpu._lib.Config), C.c_void_p, C.c_int32, C.c_int32, C.c_int32,
                   C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_float, C.c_void_p,
-                  C.c_void_p, C.c_void_p]
+                  C.c_void_p, C.c_void_p, C.c_void_p]
     return f
 
 
@@ -47,6 +47,7 @@ def _device(case):
     t = {k: torch.from_numpy(case[k]).cuda() for k in ("ph", "ep", "sz")}
     t["fit"] = torch.full((len(case["sz"]),), float("nan"), dtype=torch.float32, device="cuda")
     t["best"] = torch.full((1,), -1, dtype=torch.int32, device="cuda")
+    t["status"] = torch.full((1,), -1, dtype=torch.int32, device="cuda")
     return data, ld, t
 
 
@@ -56,7 +57,7 @@ def _call(f, case, data, ld, t, stream):
     nlin, ncol = case["rows"].shape
     return f(C.byref(cfg), data.data_ptr(), nlin, ncol, ld, t["ph"].data_ptr(),
              t["ep"].data_ptr(), t["sz"].data_ptr(), len(case["sz"]), 1e-6,
-             t["fit"].data_ptr(), t["best"].data_ptr(), stream)
+             t["fit"].data_ptr(), t["best"].data_ptr(), t["status"].data_ptr(), stream)
 
 
 @pytest.mark.parametrize("strategy,math", [("PDP", "fast"), ("PP", "parity"), ("DP", "fast")])
@@ -71,11 +72,13 @@ def test_noalloc_matches_handle_entry_point(gpu_lib, strategy, math):
     for case, (data, ld, t) in [(big, dev_big), (small, dev_small), (big, dev_big)]:
         t["fit"].fill_(float("nan"))
         t["best"].fill_(-1)
+        t["status"].fill_(-1)
         assert _call(f, case, data, ld, t, stream) == 0
         torch.cuda.synchronize()
         fit = t["fit"].cpu().numpy()
         assert np.array_equal(fit.view(np.int32), case["fit"].view(np.int32))
         assert int(t["best"].cpu()[0]) == case["best"]
+        assert int(t["status"].cpu()[0]) == 0   # every program ran, every tile arrived
 
 
 def test_noalloc_rejects_batches_beyond_the_scratch(gpu_lib):
@@ -86,6 +89,6 @@ def test_noalloc_rejects_batches_beyond_the_scratch(gpu_lib):
     data, ld, t = _device(case)
     cfg = case["ev"]._config
     st = f(C.byref(cfg), data.data_ptr(), 100, 2, ld, t["ph"].data_ptr(), t["ep"].data_ptr(),
-           t["sz"].data_ptr(), 100000, 0.0, t["fit"].data_ptr(), t["best"].data_ptr(),
+           t["sz"].data_ptr(), 100000, 0.0, t["fit"].data_ptr(), t["best"].data_ptr(), None,
            torch.cuda.current_stream().cuda_stream)
     assert st == 4   # PPI_ERR_UNSUPPORTED, nothing launched
