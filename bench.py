@@ -140,48 +140,149 @@ def profile_traffic(workload):
     return profile_value("eval_kernel_" + workload, "traffic_bytes_per_launch")
 
 
-def cpu_sample(wl, ph, eph, sz, budget_s, threads=0, chunk=0):
+def cpu_sample(wl, ph, eph, sz, budget_s, threads=0, chunk=0, alpha=1e-6):
     """Oracle port (OpenMP over programs) on the first programs of the
-    population, all records, until budget_s of work: (GPop/s, programs, cores)."""
+    population, all records, until budget_s of work:
+    (GPop/s, programs, cores, seconds, the programs' fitness)."""
     from oracle import pyoracle
     pyoracle.build()
     o = pyoracle.Oracle(wl.rows, wl.grammar.symbol_table_arrays(), wl.error_fn, wl.cost,
                         wl.reduce_max, wl.protected, False, threads)
     cores = threads if threads > 0 else (os.cpu_count() or 1)
     chunk = chunk or 2 * cores
-    done, ops, t = 0, 0, 0.0
+    done, ops, t, fits = 0, 0, 0.0, []
     while done < len(sz) and (t < budget_s or done == 0):
         k = min(chunk, len(sz) - done)
         t0 = time.perf_counter()
-        o.evaluate(ph[done:done + k], eph[done:done + k], sz[done:done + k], wl.strategy,
-                   1 if wl.strategy == "PP" else min(wl.nlin, 1024), 1e-6)
+        fits.append(o.evaluate(ph[done:done + k], eph[done:done + k], sz[done:done + k],
+                               wl.strategy, 1 if wl.strategy == "PP" else min(wl.nlin, 1024), alpha))
         t += time.perf_counter() - t0
         ops += int(sz[done:done + k].sum()) * wl.nlin
         done += k
-    return ops / t / 1e9, done, cores, t
+    return ops / t / 1e9, done, cores, t, np.concatenate(fits)
 
 
 def batch_cpu_sample(pops, sym, fraction, threads=0, slice_index=0):
     """Oracle port on a slice of every population's programs (a `fraction` of
     each, and at least one per core: the port runs programs in parallel; slice
     `slice_index` of the population, wrapping), all records:
-    (GPop/s, programs, cores, seconds)."""
+    (GPop/s, programs, cores, seconds, [(population, slice, fitness)])."""
     from oracle import pyoracle
     pyoracle.build()
     cores = threads if threads > 0 else (os.cpu_count() or 1)
-    ops, t, done = 0, 0.0, 0
-    for p in pops:
+    ops, t, done, fits = 0, 0.0, 0, []
+    for i, p in enumerate(pops):
         k = min(p["n"], max(cores, int(round(p["n"] * fraction))))
         lo = (slice_index * k) % max(1, p["n"] - k + 1)
         sl = slice(lo, lo + k)
         o = pyoracle.Oracle(p["rows"], sym, p["error_fn"], None, False, p["protected"], False, threads)
         lanes = min(p["rows"].shape[0], 1024)
         t0 = time.perf_counter()
-        o.evaluate(p["phenotype"][sl], p["ephemeral"][sl], p["size"][sl], "PDP", lanes, 0.0)
+        f = o.evaluate(p["phenotype"][sl], p["ephemeral"][sl], p["size"][sl], "PDP", lanes, 0.0)
         t += time.perf_counter() - t0
+        fits.append((i, sl, f))
         ops += int(p["size"][sl].astype(np.int64).sum()) * p["rows"].shape[0]
         done += k
-    return ops / t / 1e9, done, cores, t
+    return ops / t / 1e9, done, cores, t, fits
+
+
+# Input range of each opcode's throughput probe (others: [-3, 3]); binary
+# opcodes take the constant 1.375 as right operand.
+PROBE_DOMAIN = {"LOG": (1.0, 100.0), "LOG2": (1.0, 100.0), "LOG10": (1.0, 100.0),
+                "SQRT": (1.0, 100.0), "EXP": (-5.0, 5.0), "EXP2": (-5.0, 5.0),
+                "EXP10": (-3.0, 3.0), "GAMMA": (0.5, 5.0), "POW": (0.5, 3.0)}
+_OP_RATES = {}
+
+
+def op_rates(names, iters=8192):
+    """Gop/s of each opcode's arithmetic alone on this GPU (the evaluator's
+    fast-math routines in a register loop, libppi_opcost.so), less the loop's
+    own cost; cached for the process."""
+    import ctypes as C
+    from ppi_gpu import build as B
+    from ppi_gpu import grammar as G
+    if not os.path.exists(B.OPCOST_LIB):
+        B.build_opcost()
+    L = C.CDLL(B.OPCOST_LIB)
+    L.ppi_opcost_measure.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_float, C.c_float,
+                                     C.c_float, C.POINTER(C.c_float), C.POINTER(C.c_double)]
+
+    def measure(op, lo, hi):
+        ms, n = C.c_float(), C.c_double()
+        rc = L.ppi_opcost_measure(op, 1, iters, 3, lo, hi, 1.375, C.byref(ms), C.byref(n))
+        if rc != 0:
+            raise RuntimeError("op throughput probe failed (CUDA error %d)" % rc)
+        return ms.value, n.value
+
+    if "_loop" not in _OP_RATES:
+        _OP_RATES["_loop"] = measure(-1, -3.0, 3.0)[0]
+    for name in names:
+        if name not in _OP_RATES:
+            lo, hi = PROBE_DOMAIN.get(name, (-3.0, 3.0))
+            ms, n = measure(G.OP[name], lo, hi)
+            _OP_RATES[name] = n / max(ms - _OP_RATES["_loop"], 1e-4) / 1e6
+    return {k: _OP_RATES[k] for k in names}
+
+
+def opmix_roofline(achieved, prog_sets):
+    """Op-mix-aware ceiling of a workload: its opcode x record count divided
+    by the time its operators' arithmetic alone takes at the probed rates
+    (terminals -- attributes, constants, literals -- cost nothing, and the
+    interpreter, the tile staging and the error reduction cost nothing).
+    prog_sets: (phenotype, size, records, symbol table) per population."""
+    from ppi_gpu import grammar as G
+    hist, total = {}, 0
+    for ph, sz, nlin, (sv, so, _) in prog_sets:
+        lut = dict(zip(np.asarray(sv).tolist(), np.asarray(so).tolist()))
+        toks = ph[np.arange(ph.shape[1])[None, :] < sz[:, None]]
+        vals, counts = np.unique(toks, return_counts=True)
+        for v, c in zip(vals.tolist(), counts.tolist()):
+            op = int(lut.get(v, 0))
+            hist[op] = hist.get(op, 0) + c * int(nlin)
+        total += int(sz.astype(np.int64).sum()) * int(nlin)
+    ops = {G.OPS[o]: n for o, n in hist.items() if o >= G.OP["AND"]}
+    rates = op_rates(sorted(ops))
+    t = sum(n / (rates[k] * 1e9) for k, n in ops.items())
+    ceiling = total / t / 1e9 if t > 0 else None
+    return {"ceiling": round(ceiling, 1) if ceiling else None,
+            "frac": round(achieved / ceiling, 4) if ceiling else None, "unit": "Gop/s",
+            "terminal_share": round(1.0 - sum(ops.values()) / total, 4),
+            "op_share": {k: round(n / total, 4) for k, n in sorted(ops.items())},
+            "op_rates_gops": {k: round(v, 1) for k, v in sorted(rates.items())},
+            "how": "operators' fast-math arithmetic alone, 8 independent values per thread, "
+                   "whole GPU (libppi_opcost.so); terminals free"}
+
+
+def parity_block(gpu, ref, gpu64=None, fp64=None, what=""):
+    """Fitness of the timed GPU path against the oracle on the same programs
+    (the reference's sequential arithmetic in the same strategy's order: only
+    the transcendental functions' rounding differs in fast math), and against
+    an FP64 re-evaluation of a subsample (the error of float evaluation
+    itself).  Relative differences are over programs finite on both sides;
+    sentinel agreement is the share of programs both call non-finite or both
+    finite."""
+    gpu = np.asarray(gpu, np.float32)
+    ref = np.asarray(ref, np.float32)
+    fin = (gpu < 1e30) & (ref < 1e30)
+    rel = np.abs(gpu[fin].astype(np.float64) - ref[fin]) / np.maximum(np.abs(ref[fin]), 1e-30)
+    out = {"programs": int(len(gpu)), "against": "oracle port of the reference (sequential.cc "
+           "arithmetic, same strategy order)" + what,
+           "sentinel_agreement": round(float(((gpu >= 1e30) == (ref >= 1e30)).mean()), 5),
+           "bitexact_frac": round(float((gpu.view(np.int32) == ref.view(np.int32)).mean()), 5),
+           "max_rel_diff": float(rel.max()) if rel.size else 0.0,
+           "median_rel_diff": float(np.median(rel)) if rel.size else 0.0,
+           "frac_within_1e-5": round(float((rel <= 1e-5).mean()), 5) if rel.size else 1.0}
+    if fp64 is not None:
+        g = np.asarray(gpu64, np.float64)
+        f = np.asarray(fp64, np.float64)
+        ok = (g < 1e30) & np.isfinite(f)
+        r64 = np.abs(g[ok] - f[ok]) / np.maximum(np.abs(f[ok]), 1e-300)
+        out["fp64"] = {"programs": int(len(f)),
+                       "sentinel_agreement": round(float(((g >= 1e30) == ~np.isfinite(f)).mean()), 5),
+                       "max_rel_err": float(r64.max()) if r64.size else 0.0,
+                       "median_rel_err": float(np.median(r64)) if r64.size else 0.0,
+                       "frac_within_1e-5": round(float((r64 <= 1e-5).mean()), 5) if r64.size else 1.0}
+    return out
 
 
 def batch_config(pops, work, extra):
@@ -222,7 +323,7 @@ def run_reference(args):
     frac = args.cpu_fraction
     vals = []
     for k in range(args.warmup + args.steps):
-        v, n, cores, t = batch_cpu_sample(pops, sym, frac, slice_index=k)
+        v, n, cores, t, _ = batch_cpu_sample(pops, sym, frac, slice_index=k)
         if k >= args.warmup:
             vals.append((v, t))
     value = float(np.mean([v for v, _ in vals]))
@@ -261,7 +362,7 @@ def run_reference_single(args):
     vals = []
     for k in range(args.warmup + args.steps):
         lo = (k * per_step) % max(1, len(sz) - per_step + 1)
-        v, n, cores, t = cpu_sample(wl, ph[lo:lo + per_step], eph[lo:lo + per_step],
+        v, n, cores, t, _ = cpu_sample(wl, ph[lo:lo + per_step], eph[lo:lo + per_step],
                                     sz[lo:lo + per_step], 0.0, 0, per_step)
         if k >= args.warmup:
             vals.append((v, t))
@@ -406,7 +507,8 @@ def run_batch(args):
     peak = sm_count * 128 * max_mhz * 1e6 / 1e9          # FP32 lane-ops/s, in G
     block, grid, rows, tune = be.shape()
     kernel_ms = float(np.mean(step_ms))
-    cpu_v, cpu_n, cpu_cores, cpu_t = batch_cpu_sample(pops, sym, args.cpu_fraction)
+    cpu_v, cpu_n, cpu_cores, cpu_t, cpu_fits = batch_cpu_sample(pops, sym, args.cpu_fraction)
+    parity = batch_parity(pops, sym, fit_b, cpu_fits, offs)
     issue = profile_value("eval_batch_kernel_uneven-batch-mid", "issue_active_frac")
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world,
@@ -439,17 +541,40 @@ def run_batch(args):
                                                    (sm_count * 128 * clk["sm_mhz"] / 1e3), 4)
                      if clk.get("sm_mhz") else None,
                      "issue_active_frac": issue,
-                     "traffic": profile_traffic("uneven-batch")},
+                     "traffic": profile_traffic("uneven-batch"),
+                     "opmix": opmix_roofline(all_ops / world / (kernel_ms / 1e3) / 1e9,
+                                             [(p["phenotype"], p["size"], p["rows"].shape[0], sym)
+                                              for p in pops])},
         "cpu_baseline": {"value": round(cpu_v, 4), "unit": UNIT, "cores": cpu_cores,
                          "kind": "port",
                          "sample": "first %.1f%% (at least one per core) of every population's "
                                    "programs (%d) x all records (%.1f s), oracle port, OpenMP "
                                    "over programs" % (
                                        100 * args.cpu_fraction, cpu_n, cpu_t)},
+        "parity": parity,
         "clocks": clk,
     }
-    print(json.dumps(line))
-    return 0
+    return line
+
+
+def batch_parity(pops, sym, fit_gpu, cpu_fits, offs, fp64_per_pop=2):
+    """Parity block of the batch: the GPU fitness of the CPU sample's programs
+    against the oracle's, and of its first programs per population against
+    an FP64 re-evaluation."""
+    from oracle import pyoracle
+    gpu, ref, g64, f64 = [], [], [], []
+    for i, sl, f in cpu_fits:
+        p = pops[i]
+        gsl = fit_gpu[offs[i] + sl.start: offs[i] + sl.stop]
+        gpu.append(gsl)
+        ref.append(f)
+        k = min(fp64_per_pop, sl.stop - sl.start)
+        o = pyoracle.Oracle(p["rows"], sym, p["error_fn"], None, False, p["protected"], False)
+        sub = slice(sl.start, sl.start + k)
+        f64.append(o.evaluate64(p["phenotype"][sub], p["ephemeral"][sub], p["size"][sub]))
+        g64.append(gsl[:k])
+    return parity_block(np.concatenate(gpu), np.concatenate(ref), np.concatenate(g64),
+                        np.concatenate(f64), ", PDP over each population's 1024 lanes")
 
 
 def run_adjoint(args):
@@ -531,9 +656,10 @@ def run_adjoint(args):
             "refinement": {"steps": 5, "optimizer": "Adam lr 0.05",
                            "median_fitness_before": float(np.median(fit[keep])),
                            "median_fitness_after": float(np.median(fit_end[keep])),
-                           "improved_fraction": round(float((fit_end[keep] < fit[keep]).mean()), 4)}}
-    print(json.dumps(line))
-    return 0
+                           "improved_fraction": round(float((fit_end[keep] < fit[keep]).mean()), 4)},
+            "parity": parity_block(fit[:k], o.evaluate(ph[:k], ep[:k], sz[:k], "PDP", ev.lanes, 0.0),
+                                   fit[:k], f64, ", forward fitness of the gradient's programs")}
+    return line
 
 
 def run_polynomial(args):
@@ -635,7 +761,14 @@ def run_polynomial(args):
     eval_mean = float(np.mean(eval_ms))
     achieved = ops_per_step / (eval_mean / 1e3) / 1e9
     traffic = profile_traffic(wl.name)
-    cpu_v, cpu_n, cpu_cores, cpu_t = cpu_sample(wl, ph, eph, sz, args.cpu_seconds)
+    cpu_v, cpu_n, cpu_cores, cpu_t, cpu_fit = cpu_sample(wl, ph, eph, sz, args.cpu_seconds)
+    from oracle import pyoracle
+    k64 = min(cpu_n, args.fp64_programs)
+    f64 = pyoracle.Oracle(wl.rows, wl.grammar.symbol_table_arrays(), wl.error_fn, wl.cost,
+                          wl.reduce_max, wl.protected, False).evaluate64(ph[:k64], eph[:k64],
+                                                                         sz[:k64], 1e-6)
+    parity = parity_block(fit_host[:cpu_n], cpu_fit, fit_host[:k64], f64,
+                          ", %s over %d lanes" % (wl.strategy, ev.lanes))
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup,
@@ -655,15 +788,45 @@ def run_polynomial(args):
                      "kernel": "eval_kernel", "kernel_ms": round(eval_mean, 4),
                      "frac_at_median_clock": round(achieved / (sm_count * 128 * clk["sm_mhz"] / 1e3), 4)
                      if clk.get("sm_mhz") else None,
-                     "traffic": traffic},
+                     "traffic": traffic,
+                     "opmix": opmix_roofline(achieved, [(ph, sz, wl.nlin,
+                                                         wl.grammar.symbol_table_arrays())])},
         "cpu_baseline": {"value": round(cpu_v, 4), "unit": UNIT, "cores": cpu_cores,
                          "kind": "port",
                          "sample": "first %d programs x all %d records (%.1f s), oracle port, "
                                    "OpenMP over programs" % (cpu_n, wl.nlin, cpu_t)},
+        "parity": parity,
         "clocks": clk,
     }
-    print(json.dumps(line))
-    return 0
+    return line
+
+
+# The benchmark's other configurations, reported beside the headline in the
+# default line: (key, workload, population, records, steps at most, CPU seconds).
+SUB_CONFIGS = [("iris", "iris", 1000, 150, 5, 3.0),
+               ("polynomial", "polynomial", 30_000, 100_000, 5, 5.0),
+               ("stream", "stream", 30_000, 4_000_000, 2, 5.0),
+               ("adjoint", "adjoint", 10_000, 100_000, 5, 0.0)]
+
+
+def sub_line(line):
+    """A configuration's line without the keys the headline already states."""
+    drop = ("metric", "n_gpus", "higher_is_better", "scaling", "vs_baseline", "data", "warmup")
+    return {k: v for k, v in line.items() if k not in drop}
+
+
+def run_sub_configs(args):
+    out = {}
+    for key, workload, population, records, steps, cpu_s in SUB_CONFIGS:
+        a = argparse.Namespace(**vars(args))
+        a.workload, a.population, a.records = workload, population, records
+        a.steps, a.cpu_seconds = min(args.steps, steps), cpu_s
+        t0 = time.perf_counter()
+        line = run_adjoint(a) if workload == "adjoint" else run_polynomial(a)
+        sub = sub_line(line)
+        sub["wall_s"] = round(time.perf_counter() - t0, 1)
+        out[key] = sub
+    return out
 
 
 def main():
@@ -683,6 +846,10 @@ def main():
     ap.add_argument("--max-programs", type=int, default=30_000)
     ap.add_argument("--records", type=int, default=100_000)
     ap.add_argument("--population", type=int, default=30_000)
+    ap.add_argument("--fp64-programs", type=int, default=16,
+                    help="programs re-evaluated in FP64 for the parity block")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="default workload: skip the other configurations' sub-blocks")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
     if args.workload == "stream" and args.records == 100_000:
@@ -692,10 +859,18 @@ def main():
     if args.impl == "reference":
         return run_reference(args)
     if args.workload in ("polynomial", "iris", "stream"):
-        return run_polynomial(args)
-    if args.workload == "adjoint":
-        return run_adjoint(args)
-    return run_batch(args)
+        line = run_polynomial(args)
+    elif args.workload == "adjoint":
+        line = run_adjoint(args)
+    else:
+        line = run_batch(args)
+        # the other configurations, on one GPU only (under torchrun every rank
+        # would hold all GPUs for them)
+        if isinstance(line, dict) and dist_env()[1] == 1 and not args.no_configs:
+            line["configs"] = run_sub_configs(args)
+    if isinstance(line, dict):
+        print(json.dumps(line))
+    return 0
 
 
 if __name__ == "__main__":

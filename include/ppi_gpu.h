@@ -157,6 +157,23 @@ ppi_status ppi_gpu_set_dataset(ppi_gpu* h, const float* const* rows, int32_t nli
 /* Same, from one row-major nlin x ncol array. */
 ppi_status ppi_gpu_set_dataset_rowmajor(ppi_gpu* h, const float* data, int32_t nlin, int32_t ncol);
 
+/* Same, straight from PPI's training CSV file into the column-major device
+ * layout, read by the rules of PPI's own reader (read(), src/main.cc:32-122):
+ * empty and '#' lines skipped, ',' separated, an optional header line, values
+ * read as `istringstream >> float`, NaN / infinite / unreadable values and
+ * ragged lines rejected.  A file the reference reader rejects is rejected
+ * with PPI_ERR_INVALID_ARGUMENT and the reference's message in last_error.
+ * nlin / ncol (may be NULL) receive the shape read. */
+ppi_status ppi_gpu_set_dataset_csv(ppi_gpu* h, const char* path, int32_t* nlin, int32_t* ncol);
+
+/* The same reader without a device: shape into nlin / ncol and, when
+ * colmajor is not NULL, the values at colmajor[c * ld + r] (ld >= nlin,
+ * capacity >= ld * ncol floats); message (may be NULL) receives the reader's
+ * message.  No reference counterpart beyond read(): for callers that stage
+ * the dataset themselves (e.g. ppi_gpu_evaluate_noalloc). */
+ppi_status ppi_csv_read(const char* path, float* colmajor, int64_t capacity, int32_t ld,
+                        int32_t* nlin, int32_t* ncol, char* message, int32_t message_len);
+
 /* One generation: phenotype / ephemeral are n rows of max_size entries, size
  * holds n program lengths (0 = invalid program).  fitness[i] receives
  * error/nlin + alpha*size[i] (FLT_MAX for invalid or non-finite programs, as

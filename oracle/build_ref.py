@@ -115,6 +115,45 @@ def extract_decode(ppi_cc):
     return src[start:i + 1] + "\n"
 
 
+def extract_read(main_cc):
+    """read() of src/main.cc (lines 32-119): PPI's CSV dataset reader."""
+    src = open(main_cc).read()
+    start = src.index("int read( const std::string& dataset")
+    depth, i = 0, src.index("{", start)
+    while True:   # braces outside comments and string / character literals
+        c = src[i]
+        if src.startswith("//", i):
+            i = src.index("\n", i)
+            continue
+        if src.startswith("/*", i):
+            i = src.index("*/", i) + 2
+            continue
+        if c in "\"'":
+            j = i + 1
+            while src[j] != c:
+                j += 2 if src[j] == "\\" else 1
+            i = j + 1
+            continue
+        if c == "{":
+            depth += 1
+        elif c == "}":
+            depth -= 1
+            if depth == 0:
+                break
+        i += 1
+    return src[start:i + 1] + "\n"
+
+
+def build_csv(ref):
+    """libref_csv.so: the reference's read() + oracle/ref_csv_driver.cc."""
+    os.makedirs(OUT, exist_ok=True)
+    open(os.path.join(OUT, "csv_extract.inc"), "w").write(
+        extract_read(os.path.join(ref, "src", "main.cc")))
+    run(["g++", "-O2", "-fPIC", "-shared", "-w", "-std=c++17", "-I", OUT,
+         "-I", os.path.join(ref, "src", "util"), os.path.join(HERE, "ref_csv_driver.cc"),
+         "-o", os.path.join(OUT, "libref_csv.so")])
+
+
 def run(cmd, cwd=None):
     r = subprocess.run(cmd, cwd=cwd, capture_output=True, text=True)
     if r.returncode != 0:
@@ -174,8 +213,10 @@ def main():
     man_path = os.path.join(OUT, "manifest.json")
     manifest = json.load(open(man_path)) if os.path.exists(man_path) else {}
     with ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 1)) as ex:
+        csv = ex.submit(build_csv, a.ref)
         for name, info in ex.map(lambda n: build_one(a.ref, n, CONFIGS[n]), names):
             manifest[name] = info
+        csv.result()
     json.dump(manifest, open(man_path, "w"), indent=1)
     print("built %d reference configurations into %s" % (len(names), OUT))
     return 0

@@ -652,6 +652,119 @@ static void d_partials(int op, double a, double b, double c, double v, int prot,
    }
 }
 
+/* ---- FP64 re-evaluation (test infrastructure) ----------------------------
+ * No counterpart in the reference.  The same programs over the same float
+ * data, every node computed in double precision (double libm, the protected
+ * rules of functions.h:99-193 applied to double operands), the error function
+ * and the sum over records in double: the value the float evaluators
+ * approximate, so their error can be stated against it. */
+static double d_gamma(double x, int prot) {
+   const double e = (double)PPI_E_F, pi = (double)PPI_PI_F;
+   double s = x * sinh(1.0 / x);
+   double a = (x / e) * ((prot && s < 0.0) ? 1.0 : sqrt(s));
+   double q = 2.0 * pi / x;
+   return pow(a, x) * ((prot && q < 0.0) ? 1.0 : sqrt(q));
+}
+
+static double d_node(int op, double a, double b, double c, int prot) {
+   if (op == OP_GAMMA) return d_gamma(a, prot);
+   if (op == OP_TAN && prot &&
+       (fabs(a) == (double)PPI_PI_2_F || fabs(a) == (double)(3.0f * PPI_PI_2_F)))
+      return 1.0;
+   return d_value(op, a, b, c, prot);
+}
+
+static double eval_record64(const int* ops, const float* lit, int size, const float* row, int ncol,
+                            int prot, double* stack) {
+   int top = -1;
+   for (int i = size - 1; i >= 0; --i) {
+      int op = ops[i], ar = arity(op);
+      if (ar > 0 && top + 1 < ar) {
+         int have = top + 1, miss = ar - have;
+         for (int k = have - 1; k >= 0; --k) stack[k + miss] = stack[k];
+         for (int k = 0; k < miss; ++k) stack[k] = NAN;
+         top = ar - 1;
+      }
+      if (ar == 0) {
+         double v;
+         if (op == OP_ATTRIBUTE) {
+            float x = lit[i];
+            v = (x >= 0.0f && x < (float)ncol) ? (double)row[(int)x] : NAN;
+         } else if (op == OP_INVALID) {
+            v = NAN;
+         } else {
+            v = (double)lit[i];
+         }
+         stack[++top] = v;
+         continue;
+      }
+      double a = stack[top], b = ar > 1 ? stack[top - 1] : 0.0, cc = ar > 2 ? stack[top - 2] : 0.0;
+      top -= ar - 1;
+      stack[top] = d_node(op, a, b, cc, prot);
+   }
+   return top >= 0 ? stack[top] : NAN;
+}
+
+static double error_fn64(const ppio_config* c, double x, double y) {
+   switch (c->error_fn) {
+   case 0: return fabs(x - y);
+   case 1: return (x - y) * (x - y);
+   case 2: return (x != y) ? 1.0 : 0.0;
+   case 3: {
+      if (x != x) return NAN;
+      int n = c->cost_n;
+      int ix = x >= (double)n ? n - 1 : (x > 0.0 ? (int)x : 0);
+      int iy = y != y ? 0 : (y >= (double)n ? n - 1 : (y > 0.0 ? (int)y : 0));
+      return (double)c->cost[ix * n + iy];
+   }
+   }
+   return NAN;
+}
+
+int ppio_evaluate64(const ppio_config* c, const int32_t* phenotype, const float* ephemeral,
+                    const int32_t* size, int max_size, int n, double alpha, double* fitness) {
+   int failed = 0;
+#ifdef _OPENMP
+   int nt = c->threads > 0 ? c->threads : omp_get_max_threads();
+#pragma omp parallel num_threads(nt)
+#endif
+   {
+      int* ops = (int*)malloc(sizeof(int) * (size_t)(max_size + 1));
+      float* lit = (float*)malloc(sizeof(float) * (size_t)(max_size + 1));
+      double* stack = (double*)malloc(sizeof(double) * (size_t)(max_size + 4));
+      if (!ops || !lit || !stack) {
+         failed = 1;
+      } else {
+#ifdef _OPENMP
+#pragma omp for schedule(dynamic, 1)
+#endif
+         for (int i = 0; i < n; ++i) {
+            int sz = size[i];
+            if (sz <= 0 || sz > max_size) { fitness[i] = HUGE_VAL; continue; }
+            map_program(c, phenotype + (size_t)i * max_size, ephemeral + (size_t)i * max_size, sz,
+                        ops, lit);
+            double sum = 0.0;
+            int nonfin = 0;
+            for (int r = 0; r < c->nlin; ++r) {
+               const float* row = c->rows + (size_t)r * c->ncol;
+               double x = eval_record64(ops, lit, sz, row, c->ncol, c->protected_fns, stack);
+               double e = error_fn64(c, x, (double)row[c->ncol - 1]);
+               if (isinf(e) || isnan(e)) { nonfin = 1; break; }
+               if (c->reduce_max) {
+                  double m = e * (double)c->nlin;
+                  sum = m > sum ? m : sum;
+               } else {
+                  sum += e;
+               }
+            }
+            fitness[i] = nonfin ? HUGE_VAL : sum / (double)c->nlin + alpha * (double)sz;
+         }
+      }
+      free(ops); free(lit); free(stack);
+   }
+   return failed;
+}
+
 int ppio_adjoint64(const ppio_config* c, const int32_t* phenotype, const double* ephemeral,
                    const int32_t* size, int max_size, int n, int float_forward, double* fitness,
                    double* grad) {

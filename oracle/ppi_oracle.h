@@ -58,6 +58,14 @@ int ppio_best_index(const float* fitness, int n);
  * per-program values, DP the alpha-included fitness. */
 int ppio_best_index_accelerator(const float* values, int n, int group);
 
+/* FP64 re-evaluation (no counterpart in the reference): every node, the error
+ * function and the record sum in double precision, records in order;
+ * fitness[i] = sum/nlin + alpha*size[i] (REDUCEMAX: the max of error*nlin),
+ * HUGE_VAL for size 0 or a non-finite error.  The value the float evaluators
+ * approximate. */
+int ppio_evaluate64(const ppio_config* cfg, const int32_t* phenotype, const float* ephemeral,
+                    const int32_t* size, int max_size, int n, double alpha, double* fitness);
+
 /* Genome decode (src/ppi.cc:106-182).  Tables as returned by
  * ppi_gpu.grammar.Grammar.decode_tables().  genomes: n x nb bytes of 0/1.
  * Rows of phenotype/ephemeral hold max_size entries.  Returns 0. */

@@ -65,6 +65,8 @@ def lib():
         L.ppio_predict.argtypes = [C.POINTER(_Cfg), _ip, _fp, C.c_int, _fp]
         L.ppio_best_index.argtypes = [_fp, C.c_int]
         L.ppio_best_index_accelerator.argtypes = [_fp, C.c_int, C.c_int]
+        L.ppio_evaluate64.argtypes = [C.POINTER(_Cfg), _ip, _fp, _ip, C.c_int, C.c_int, C.c_double,
+                                      C.POINTER(C.c_double)]
         _dp = C.POINTER(C.c_double)
         L.ppio_adjoint64.argtypes = [C.POINTER(_Cfg), _ip, _dp, _ip, C.c_int, C.c_int, C.c_int, _dp,
                                      _dp]
@@ -99,6 +101,18 @@ class Oracle:
         rc = lib().ppio_evaluate(C.byref(self.cfg), STRATEGY[strategy], lanes, _i(ph), _f(ep),
                                  _i(sz), mps, n, alpha, _f(out))
         assert rc == 0
+        return out
+
+    def evaluate64(self, phenotype, ephemeral, size, alpha=0.0):
+        """FP64 re-evaluation (ppio_evaluate64): double fitness, HUGE_VAL
+        (inf) where the float evaluators give the FLT_MAX sentinel's cases."""
+        ph = np.ascontiguousarray(phenotype, np.int32)
+        ep = np.ascontiguousarray(ephemeral, np.float32)
+        sz = np.ascontiguousarray(size, np.int32)
+        n, mps = ph.shape
+        out = np.empty(n, np.float64)
+        assert lib().ppio_evaluate64(C.byref(self.cfg), _i(ph), _f(ep), _i(sz), mps, n, alpha,
+                                     out.ctypes.data_as(C.POINTER(C.c_double))) == 0
         return out
 
     def adjoint64(self, phenotype, ephemeral, size, float_forward=False):
@@ -153,6 +167,25 @@ def decode(grammar, genomes, bits_per_gene, bits_per_constant, lo, hi, max_size)
 
 
 # ---- reference builds (oracle/_ref, present only where the reference was built) ----
+
+def ref_csv_read(path):
+    """The reference's own read() (src/main.cc:32-119): (status, array or
+    None).  Its messages go to stderr, as in PPI.  None when oracle/_ref has
+    no CSV build."""
+    so = os.path.join(REF, "libref_csv.so")
+    if not os.path.exists(so):
+        return None
+    L = C.CDLL(so)
+    L.ref_csv_read.argtypes = [C.c_char_p, _fp, C.c_long, _ip, _ip]
+    nlin = np.zeros(1, np.int32)
+    ncol = np.zeros(1, np.int32)
+    rc = L.ref_csv_read(os.fsencode(path), None, 0, _i(nlin), _i(ncol))
+    if rc != 0:
+        return rc, None
+    out = np.zeros((int(nlin[0]), int(ncol[0])), np.float32)
+    rc = L.ref_csv_read(os.fsencode(path), _f(out), out.size, _i(nlin), _i(ncol))
+    return rc, out
+
 
 def ref_manifest():
     p = os.path.join(REF, "manifest.json")

@@ -79,6 +79,7 @@ struct State {
 
 struct Options {
    std::string strategy = "PDP";
+   std::string dataset;      // -d / --dataset: the CSV main.cc read (src/main.cc:141,152)
    int lanes = -1, device = 0;
    bool verbose = false, ok = true;
 };
@@ -102,6 +103,8 @@ Options parse(int argc, char** argv) {
          else { std::fprintf(stderr, "Valid strategy: PP, DP and PDP.\n"); o.ok = false; }
       } else if ((a == "-cl-mls" || a == "--cl-max-local-size") && has_value) {
          o.lanes = std::atoi(argv[++i]);
+      } else if ((a == "-d" || a == "--dataset") && has_value) {
+         o.dataset = argv[++i];
       } else if ((a == "-cl-d" || a == "--cl-device-id") && has_value) {
          o.device = std::max(0, std::atoi(argv[++i]));
       } else if ((a == "-type") && has_value) {
@@ -193,16 +196,28 @@ int acc_interpret_init(int argc, char** argv, const unsigned size, const unsigne
       std::fprintf(stderr, "Error in CUDA initialization phase (status %d).\n", (int)s);
       return 1;
    }
-   s = ppi_gpu_set_dataset(data.h, input, nlin, ncol);
-   if (s != PPI_OK) {
-      std::fprintf(stderr, "Error in build the kernel: %s\n", ppi_gpu_last_error(data.h));
-      return 1;
+   // The dataset: straight from the CSV file main.cc read (the same reader
+   // rules, columns written in the device layout) when the command line names
+   // it and it gives main.cc's shape; else from main.cc's float** rows.
+   bool from_file = false;
+   if (!o.dataset.empty()) {
+      int32_t rows = 0, cols = 0;
+      from_file = ppi_gpu_set_dataset_csv(data.h, o.dataset.c_str(), &rows, &cols) == PPI_OK &&
+                  rows == nlin && cols == ncol;
+   }
+   if (!from_file) {
+      s = ppi_gpu_set_dataset(data.h, input, nlin, ncol);
+      if (s != PPI_OK) {
+         std::fprintf(stderr, "Error in build the kernel: %s\n", ppi_gpu_last_error(data.h));
+         return 1;
+      }
    }
    data.nlin = nlin;
    data.verbose = o.verbose;
    if (o.verbose)
-      std::printf("\nDevice: CUDA %d (%s), strategy %s, work-items per program/group: %d\n", o.device,
-                  ppi_gpu_version(), o.strategy.c_str(), (int)ppi_gpu_lanes(data.h));
+      std::printf("\nDevice: CUDA %d (%s), strategy %s, work-items per program/group: %d, dataset %s\n",
+                  o.device, ppi_gpu_version(), o.strategy.c_str(), (int)ppi_gpu_lanes(data.h),
+                  from_file ? "read from the CSV file" : "from the host rows");
    (void)prediction_mode;
    return 0;
 }

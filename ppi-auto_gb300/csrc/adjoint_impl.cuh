@@ -261,7 +261,43 @@ __global__ void __launch_bounds__(128, 4) adjoint_kernel(const AdjointArgs a) {
          continue;
       }
       const uint2* code = a.code + (size_t)prog * a.code_stride;
-      for (int k = tid; k < meta.y; k += P) s_code[k] = code[k];
+      // The forward bytecode [ch + 2, rev) runs on the evaluator's
+      // interpreter, whose dispatch admits its own cases only: the copy
+      // checks the layout (header rows inside the tile, the sections inside
+      // the code, the constants inside the partial-sum rows) and each forward
+      // instruction as ev::load_code does, and ends the forward code with
+      // M_END at rev - 1.  A program whose layout fails is skipped (status).
+      const int rows0 = meta.x >> 8;
+      const uint2 h0 = code[0];
+      const int ch0 = code_header((int)h0.x);
+      const uint2 ah0 = ch0 + 1 < meta.y ? code[ch0] : make_uint2(0u, 0u);
+      const uint2 ah1 = ch0 + 1 < meta.y ? code[ch0 + 1] : make_uint2(0u, 0u);
+      const bool layout_ok = meta.y <= a.code_words && h0.x <= 0xFFFFu &&
+                             (int)h0.x + (int)(h0.y & 0xFFFFu) + 1 <= rows0 &&
+                             (int)ah0.x > ch0 + 2 && ah0.x < ah0.y && (int)ah0.y <= meta.y &&
+                             (int)ah1.x <= a.max_consts;
+      if (!layout_ok) {
+         if (tid == 0) {
+            atomicOr(a.status, kStatusBadInstruction);
+            a.pbad[(size_t)prog * a.n_chunks + chunk] = 1;
+         }
+         __syncthreads();
+         continue;
+      }
+      bool bad = false;
+      for (int k = tid; k < meta.y; k += P) {
+         uint2 w = code[k];
+         if (k >= ch0 + 2 && k < (int)ah0.x) {
+            const bool ok = k == (int)ah0.x - 1 ? w.x == (uint32_t)M_END
+                                                : ev::instruction_ok<OPSET>(w, rows0, a.ncol, false);
+            if (!ok) {
+               w = make_uint2((uint32_t)M_END, 0u);
+               bad = true;
+            }
+         }
+         s_code[k] = w;
+      }
+      if (bad) atomicOr(a.status, kStatusBadInstruction);
       __syncthreads();
       const uint2 hdr = s_code[0];
       const int ch = code_header((int)hdr.x);
@@ -286,7 +322,7 @@ __global__ void __launch_bounds__(128, 4) adjoint_kernel(const AdjointArgs a) {
             break;
          }
          float p[R];
-         ev::run_fast<MATH, R, OPSET, 0>(fwd, mine, T, P, tid, none, p, a.prot, a.status);
+         ev::run_fast<MATH, R, OPSET, 0>(fwd, mine, T, P, tid, none, p, a.prot);
          // error derivative: the root's adjoint
          float ys[R], g[R];
          load_row(mine + (size_t)trow * T, P, ys);

@@ -127,6 +127,46 @@ __device__ __forceinline__ void store_row(float* p, int P, const float (&x)[R]) 
    X(PPI_OP_COS) X(PPI_OP_SQRT) X(PPI_OP_LOG)
 #define PPI_ARITH_BINARY(X) X(PPI_OP_ADD) X(PPI_OP_SUB) X(PPI_OP_MULT) X(PPI_OP_DIV)
 
+// Membership in a set, from the same lists the kernels' cases come from.
+#define PPI_IS_OP(OP) op == (OP) ||
+__host__ __device__ constexpr bool arith_unary(int op) { return PPI_ARITH_UNARY(PPI_IS_OP) false; }
+__host__ __device__ constexpr bool arith_binary(int op) { return PPI_ARITH_BINARY(PPI_IS_OP) false; }
+__host__ __device__ constexpr bool full_unary(int op) { return PPI_FULL_UNARY(PPI_IS_OP) false; }
+__host__ __device__ constexpr bool full_binary(int op) { return PPI_FULL_BINARY(PPI_IS_OP) false; }
+#undef PPI_IS_OP
+
+// Instruction ids that the kernel of opcode set OPSET has a case for.
+template <int OPSET>
+__host__ __device__ constexpr bool opset_has(uint32_t id) {
+   if (id == M_END || id == M_LD_ROW || id == M_LD_C || id == M_PUSH || id == M_PUSH_LD) return true;
+   if (id >= M_UN && id < M_BR_L) {
+      const int op = PPI_OP_NOT + (int)(id - M_UN);
+      return OPSET == kOpsetArith ? arith_unary(op) : full_unary(op);
+   }
+   if (id >= M_BR_L && id < M_ITE) {
+      const int op = PPI_OP_AND + (int)((id - M_BR_L) % 18u);
+      return OPSET == kOpsetArith ? arith_binary(op) : full_binary(op);
+   }
+   return OPSET == kOpsetFull && id >= M_ITE && id < M_PUSH_LD;
+}
+
+// True when instruction w can run in a kernel of opcode set OPSET over a
+// tile of `rows` rows: its id is one of the kernel's cases, and every operand
+// it names is a row of the tile or, where the kernel reads columns directly
+// (direct), a column of the dataset.
+template <int OPSET>
+__device__ __forceinline__ bool instruction_ok(uint2 w, int rows, int ncol, bool direct) {
+   const uint32_t id = w.x, imm = w.y, nrows = (uint32_t)rows;
+   if (!opset_has<OPSET>(id)) return false;
+   if (id == M_LD_ROW || (id >= M_BR_L && id < M_BC_L)) {
+      if (imm & kDirectColumn) return direct && (imm & ~kDirectColumn) < (uint32_t)ncol;
+      return imm < nrows;
+   }
+   if (id == M_PUSH) return imm < nrows;
+   if (id == M_PUSH_LD || (id >= M_ITE && id < M_PUSH_LD)) return (imm & 0xFFFFu) < nrows && (imm >> 16) < nrows;
+   return true;
+}
+
 // Unary opcodes whose fast-math routine is long enough that R inlined copies
 // per case crowd the instruction cache (the interpreter is bound by
 // instruction fetch): their case rotates the R values through one copy.
@@ -165,19 +205,65 @@ __device__ constexpr bool roll_unary() {
 
 template <int MATH, int R, int OPSET, int D>
 __device__ __forceinline__ void run_fast(const uint2* __restrict__ code, float* mine, int T, int P,
-                                         int tid, const Direct& g, float (&acc)[R], int prot,
-                                         int* status) {
-   if constexpr (OPSET == kOpsetArith) run_fast_arith<MATH, R, D>(code, mine, T, P, tid, g, acc, prot, status);
-   else run_fast_full<MATH, R, D>(code, mine, T, P, tid, g, acc, prot, status);
+                                         int tid, const Direct& g, float (&acc)[R], int prot) {
+   if constexpr (OPSET == kOpsetArith) run_fast_arith<MATH, R, D>(code, mine, T, P, tid, g, acc, prot);
+   else run_fast_full<MATH, R, D>(code, mine, T, P, tid, g, acc, prot);
 }
 
-// Copies a program's code (meta.y words) into shared memory and puts an end
-// marker after it (the region holds code_stride + 1 words), so neither
-// interpreter can walk past the code.
-__device__ __forceinline__ void load_code(uint2* s_code, const uint2* code, int2 meta, int tid, int P) {
-   for (int i = tid; i < meta.y; i += P) s_code[i] = code[i];
-   if (tid == 0)
-      s_code[meta.y] = make_uint2(meta_kind(meta) == kKindGeneric ? kGenericEnd : (uint32_t)M_END, 0u);
+// Copies a program's code (meta.y words) into shared memory, once per
+// program, checking it on the way.  The header must leave the staged columns
+// and the target inside the tile's `rows` rows and the column list inside the
+// code; listed columns must be columns of the dataset (ncol); an instruction
+// must be one of the kernel's cases and name operands inside the tile or,
+// where the kernel reads columns directly (direct), the dataset; a
+// generic-form token must be in the op table, an attribute inside the
+// dataset.  A bad instruction or token becomes the end marker, a bad column
+// column 0, a bad header an empty program, and kStatusBadInstruction is
+// recorded.  An end marker also follows the code (`cap`: words the region
+// holds, at least meta.y + 1).  So whatever the code buffer holds, the
+// interpreters' dispatch and their shared-memory and dataset accesses stay
+// inside what the kernel has.  All threads call it; the caller synchronises
+// before reading s_code.
+template <int OPSET>
+__device__ __forceinline__ void load_code(uint2* s_code, const uint2* code, int2 meta, int cap, int rows,
+                                          int ncol, bool direct, int* status, int tid, int P) {
+   const bool generic = meta_kind(meta) == kKindGeneric;
+   const uint2 end = make_uint2(generic ? kGenericEnd : (uint32_t)M_END, 0u);
+   const uint2 hdr = code[0];
+   const int k = (int)hdr.x, s = (int)(hdr.y & 0xFFFFu), d = (int)(hdr.y >> 16);
+   const int first = generic ? 1 : code_header(k + d);
+   const bool hdr_ok = meta.y >= 2 && meta.y < cap &&
+                       (generic ? hdr.x == 0u && hdr.y == 0u
+                                : (hdr.x <= 0xFFFFu && k + s + 1 <= rows && first < meta.y));
+   if (!hdr_ok) {
+      if (tid == 0) {
+         s_code[0] = make_uint2(0u, 0u);
+         s_code[1] = end;
+         atomicOr(status, kStatusBadInstruction);
+      }
+      return;
+   }
+   bool bad = false;
+   for (int i = tid; i < meta.y; i += P) {
+      uint2 w = code[i];
+      if (i >= first) {
+         const bool ok = generic ? (w.x == kGenericEnd ||
+                                    (w.x < (uint32_t)PPI_OP_COUNT &&
+                                     (w.x != (uint32_t)PPI_OP_ATTRIBUTE || w.y < (uint32_t)ncol)))
+                                 : instruction_ok<OPSET>(w, rows, ncol, direct);
+         if (!ok) {
+            w = end;
+            bad = true;
+         }
+      } else if (i > 0) {
+         // column-list entry i holds columns 2(i-1) and 2(i-1)+1 of the k + d listed
+         if (w.x >= (uint32_t)ncol) { w.x = 0u; bad = true; }
+         if (2 * i <= k + d && w.y >= (uint32_t)ncol) { w.y = 0u; bad = true; }
+      }
+      s_code[i] = w;
+   }
+   if (bad) atomicOr(status, kStatusBadInstruction);
+   if (tid == 0) s_code[meta.y] = end;
 }
 
 // ---- generic stack interpreter ----------------------------------------------
@@ -217,6 +303,7 @@ __device__ __noinline__ void run_generic(const uint2* __restrict__ code, const f
 #pragma unroll 1
    for (int r = 0; r < R; ++r) {
       int top = -1;
+      bool overflow = false;
       const int rec = tile_pos(tid, r, P);
 #pragma unroll 1
       for (int pc = 0;; ++pc) {
@@ -224,6 +311,10 @@ __device__ __noinline__ void run_generic(const uint2* __restrict__ code, const f
          const int op = (int)ins.x;
          if (ins.x == kGenericEnd) break;
          const int ar = op_arity(op);
+         if (ar == 0 && top + 1 >= kGenericStack) {   // deeper than the translator admits
+            overflow = true;
+            break;
+         }
          if (top + 1 < ar) {
             const int have = top + 1, miss = ar - have;
             for (int k = have - 1; k >= 0; --k) stk[k + miss] = stk[k];
@@ -245,7 +336,7 @@ __device__ __noinline__ void run_generic(const uint2* __restrict__ code, const f
             stk[top] = generic_op<MATH>(op, stk[top], 0.0f, prot);
          }
       }
-      out[r] = top >= 0 ? stk[top] : qnan;
+      out[r] = (top >= 0 && !overflow) ? stk[top] : qnan;
    }
 }
 
@@ -422,6 +513,7 @@ struct Job {
    int size;
    const uint2* code;          // in global memory
    int rows_cap;               // tile rows of this pass (lane accumulators follow them)
+   int code_cap;               // words of the shared-memory code region
    int alpha_free;             // the best index compares error/nlin without alpha*size
 };
 
@@ -468,10 +560,11 @@ __device__ float evaluate_program(const Job& j, uint2* s_code, float* s_tile, in
       __syncthreads();
       return fit;
    }
-   load_code(s_code, j.code, j.meta, tid, P);
+   load_code<OPSET>(s_code, j.code, j.meta, j.code_cap, j.rows_cap, j.ncol, D != 0, status, tid, P);
    if (!aligned)
       for (int l = tid; l < L; l += P) { s_acc[l] = 0.0f; s_done[l] = 0; }
-   const uint2 hdr = j.code[0];
+   __syncthreads();
+   const uint2 hdr = s_code[0];   // as load_code checked it
    const uint2* prog = s_code + code_header((int)hdr.x + (int)(hdr.y >> 16));
    const int trow = (int)hdr.x + (int)(hdr.y & 0xFFFFu);
    float lacc[R];
@@ -492,7 +585,7 @@ __device__ float evaluate_program(const Job& j, uint2* s_code, float* s_tile, in
       float v[R];
       if (kind != kKindGeneric) {
          const Direct g{j.data + base, j.ld, j.ld - base, (base & 3) == 0};
-         run_fast<MATH, R, OPSET, D>(prog, s_tile + tid * 4, T, P, tid, g, v, j.prot, status);
+         run_fast<MATH, R, OPSET, D>(prog, s_tile + tid * 4, T, P, tid, g, v, j.prot);
       } else {
          float tmp[R];
          run_generic<MATH, R>(prog, j.data, j.ld, base, P, tid, tmp, j.prot);
@@ -607,6 +700,7 @@ __global__ void __launch_bounds__(128, min_ctas_per_sm(MATH)) eval_kernel(const 
    j.strategy = a.strategy; j.lanes = a.lanes; j.ef = a.ef; j.reduce_max = a.reduce_max;
    j.prot = a.prot; j.cost = a.cost; j.cost_n = a.cost_n; j.alpha = a.alpha;
    j.rows_cap = a.rows;
+   j.code_cap = a.code_stride + 1;
    j.alpha_free = a.best.alpha_free;
    unsigned* queue = a.wide_pass ? &a.stats->wide_queue : &a.stats->queue;
    const int limit = a.wide_pass ? (int)a.stats->wide : a.n;
@@ -677,6 +771,7 @@ __global__ void __launch_bounds__(128, min_ctas_per_sm(MATH)) eval_batch_kernel(
       j.size = a.size[g];
       j.code = a.code + (size_t)g * a.code_stride;
       j.rows_cap = a.rows;
+      j.code_cap = a.code_stride + 1;
       j.alpha_free = pd.best.alpha_free;
       float sel;
       bool abort = false;
@@ -711,10 +806,11 @@ __global__ void __launch_bounds__(128, 4) predict_kernel(const PredictArgs a) {
    const int2 m = a.meta[0];
    uint2* s_code = reinterpret_cast<uint2*>(smem_raw);
    float* s_tile = reinterpret_cast<float*>(smem_raw + code_bytes(m.y));
-   load_code(s_code, a.code, m, tid, P);
    const int kind = meta_kind(m);
    const bool runs = kind == kKindFast || kind == kKindWide || kind == kKindGeneric;
-   const uint2 hdr = runs ? a.code[0] : make_uint2(0u, 0u);
+   if (runs) load_code<OPSET>(s_code, a.code, m, m.y + 1, a.rows, a.ncol, true, a.status, tid, P);
+   __syncthreads();
+   const uint2 hdr = runs ? s_code[0] : make_uint2(0u, 0u);
    const uint2* prog = s_code + (runs ? code_header((int)hdr.x + (int)(hdr.y >> 16)) : 0);
    for (int base = blockIdx.x * T; base < a.nlin; base += gridDim.x * T) {
       __syncthreads();
@@ -723,7 +819,7 @@ __global__ void __launch_bounds__(128, 4) predict_kernel(const PredictArgs a) {
       float v[R];
       if (kind == kKindFast || kind == kKindWide) {
          const Direct g{a.data + base, a.ld, a.ld - base, (base & 3) == 0};
-         run_fast<MATH, R, OPSET, 1>(prog, s_tile + tid * 4, T, P, tid, g, v, a.prot, a.status);
+         run_fast<MATH, R, OPSET, 1>(prog, s_tile + tid * 4, T, P, tid, g, v, a.prot);
       } else if (kind == kKindGeneric) {
          float tmp[R];
          run_generic<MATH, R>(prog, a.data, a.ld, base, P, tid, tmp, a.prot);

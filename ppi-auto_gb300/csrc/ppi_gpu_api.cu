@@ -17,6 +17,12 @@
 
 using namespace ppi;
 
+namespace ppi {
+// PPI's CSV reader (dataset_csv.cu): 0, or 1 / 2 with the reference's message.
+int read_csv(const char* path, std::vector<float>* colmajor, int pad, int* rows, int* cols,
+             std::string* msg);
+}
+
 struct ppi_gpu {
    ppi_gpu_config cfg{};
    std::vector<float> cost;
@@ -141,6 +147,30 @@ ppi_status device_status(ppi_gpu* h, int bits) {
    if (bits & kStatusUnsupportedProgram)
       return fail(h, PPI_ERR_UNSUPPORTED,
                   "a malformed program needs a deeper stack than the generic interpreter's");
+   return PPI_OK;
+}
+
+// Upload of a column-major, ld-padded dataset and the geometry that follows
+// from it.
+ppi_status install_dataset(ppi_gpu* h, const std::vector<float>& cm, int nlin, int ncol, int ld) {
+   PPI_CUDA(h, cudaSetDevice(h->device));
+   cudaFree(h->d_data);
+   h->d_data = nullptr;
+   h->have_data = false;
+   PPI_CUDA(h, dalloc(&h->d_data, cm.size()));
+   PPI_CUDA(h, cudaMemcpy(h->d_data, cm.data(), cm.size() * sizeof(float), cudaMemcpyHostToDevice));
+   cudaFree(h->d_pred);
+   h->d_pred = nullptr;
+   PPI_CUDA(h, dalloc(&h->d_pred, (size_t)nlin));
+   h->nlin = nlin;
+   h->ncol = ncol;
+   h->ld = ld;
+   const int L = resolve_lanes(h->cfg.strategy, h->cfg.lanes, nlin, h->sm_count);
+   if (L < 1 || L > kMaxLanes) return fail(h, PPI_ERR_UNSUPPORTED, "lane count out of range");
+   h->lanes = L;
+   ppi_status s = plan(h);
+   if (s != PPI_OK) return s;
+   h->have_data = true;
    return PPI_OK;
 }
 
@@ -291,7 +321,6 @@ ppi_status ppi_gpu_set_dataset(ppi_gpu* h, const float* const* rows, int32_t nli
    if (!rows || nlin < 1 || ncol < 1 || ncol > kMaxColumns)
       return fail(h, PPI_ERR_INVALID_ARGUMENT, "bad dataset");
    if (h->pending) return fail(h, PPI_ERR_NOT_READY, "an evaluate_launch is still pending");
-   PPI_CUDA(h, cudaSetDevice(h->device));
    const int ld = (nlin + kColumnPad - 1) / kColumnPad * kColumnPad;
    // Column-major copy (the reference's -transpose layout, accelerator.cc:413-419),
    // zero-padded to a multiple of kColumnPad records.
@@ -300,24 +329,25 @@ ppi_status ppi_gpu_set_dataset(ppi_gpu* h, const float* const* rows, int32_t nli
       if (!rows[i]) return fail(h, PPI_ERR_INVALID_ARGUMENT, "null dataset row");
       for (int j = 0; j < ncol; ++j) cm[(size_t)j * ld + i] = rows[i][j];
    }
-   cudaFree(h->d_data);
-   h->d_data = nullptr;
-   h->have_data = false;
-   PPI_CUDA(h, dalloc(&h->d_data, cm.size()));
-   PPI_CUDA(h, cudaMemcpy(h->d_data, cm.data(), cm.size() * sizeof(float), cudaMemcpyHostToDevice));
-   cudaFree(h->d_pred);
-   h->d_pred = nullptr;
-   PPI_CUDA(h, dalloc(&h->d_pred, (size_t)nlin));
-   h->nlin = nlin;
-   h->ncol = ncol;
-   h->ld = ld;
-   const int L = resolve_lanes(h->cfg.strategy, h->cfg.lanes, nlin, h->sm_count);
-   if (L < 1 || L > kMaxLanes) return fail(h, PPI_ERR_UNSUPPORTED, "lane count out of range");
-   h->lanes = L;
-   ppi_status s = plan(h);
-   if (s != PPI_OK) return s;
-   h->have_data = true;
-   return PPI_OK;
+   return install_dataset(h, cm, nlin, ncol, ld);
+}
+
+ppi_status ppi_gpu_set_dataset_csv(ppi_gpu* h, const char* path, int32_t* nlin, int32_t* ncol) {
+   if (!h) return PPI_ERR_INVALID_ARGUMENT;
+   if (!path) return fail(h, PPI_ERR_INVALID_ARGUMENT, "null path");
+   if (h->pending) return fail(h, PPI_ERR_NOT_READY, "an evaluate_launch is still pending");
+   std::vector<float> cm;
+   std::string msg;
+   int rows = 0, cols = 0;
+   if (read_csv(path, &cm, kColumnPad, &rows, &cols, &msg) != 0)
+      return fail(h, PPI_ERR_INVALID_ARGUMENT, msg);
+   if (rows < 1 || cols < 1 || cols > kMaxColumns) return fail(h, PPI_ERR_INVALID_ARGUMENT, "empty dataset");
+   const ppi_status s = install_dataset(h, cm, rows, cols, (rows + kColumnPad - 1) / kColumnPad * kColumnPad);
+   if (s == PPI_OK) {
+      if (nlin) *nlin = rows;
+      if (ncol) *ncol = cols;
+   }
+   return s;
 }
 
 ppi_status ppi_gpu_evaluate_launch(ppi_gpu* h, const int32_t* ph, const float* eph,
@@ -406,6 +436,7 @@ ppi_status ppi_gpu_predict(ppi_gpu* h, const int32_t* ph, const float* eph, int3
    p.data = h->d_data; p.nlin = h->nlin; p.ncol = h->ncol; p.ld = h->ld;
    p.code = h->d_code; p.meta = h->d_meta; p.prot = h->cfg.protected_fns ? 1 : 0; p.out = h->d_pred;
    p.status = h->d_status;   // zeroed by the translator
+   p.rows = rows;
    const int tiles = (h->nlin + P * R - 1) / (P * R);
    const int grid = std::max(1, std::min(tiles, 4 * h->sm_count));
    PPI_CUDA(h, cudaEventRecord(h->ev0, h->stream));

@@ -437,6 +437,7 @@ struct PredictArgs {
    int prot;
    float* out;
    int* status;                // kStatus* bits
+   int rows;                   // tile rows of the launch
 };
 
 // ---------------------------------------------------------------------------

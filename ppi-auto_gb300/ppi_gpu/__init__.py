@@ -6,4 +6,4 @@ built, importing the binding raises: there is no CPU fallback.
 """
 from .grammar import Grammar, load as load_grammar, parse_bnf  # noqa: F401
 from ._lib import (Evaluator, BatchEvaluator, BATCH_GRAPH, BATCH_AUTOTUNE, PpiGpuError, STRATEGY, ERROR_FN, MATH,  # noqa: F401
-                   exported_symbols, lib_path, load_library)
+                   exported_symbols, lib_path, load_library, read_csv)

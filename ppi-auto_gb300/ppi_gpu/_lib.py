@@ -105,6 +105,9 @@ def load_library():
     L.ppi_gpu_last_stage_ms.argtypes = [C.c_void_p, _fp, _fp]
     L.ppi_gpu_lanes.argtypes = [C.c_void_p]
     L.ppi_gpu_translation.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_uint32), _ip, _ip, _ip]
+    L.ppi_gpu_set_dataset_csv.argtypes = [C.c_void_p, C.c_char_p, _ip, _ip]
+    L.ppi_csv_read.argtypes = [C.c_char_p, _fp, C.c_int64, C.c_int32, _ip, _ip, C.c_char_p,
+                               C.c_int32]
     L.ppi_gpu_kernel_arch.restype = C.c_int32
     L.ppi_gpu_constant_gradient.argtypes = [C.c_void_p, _ip, _fp, _ip, C.c_int32, _fp]
     L.ppi_batch_create.argtypes = [C.POINTER(Config), C.c_int32, C.POINTER(BatchPopulation),
@@ -128,7 +131,26 @@ def exported_symbols(header=None):
     """Function names declared in include/ppi_gpu.h (for export checks)."""
     header = header or os.path.join(_build.INCLUDE, "ppi_gpu.h")
     text = open(header).read()
-    return sorted(set(re.findall(r"\b(ppi_(?:gpu|batch)_\w+)\s*\(", text)))
+    return sorted(set(re.findall(r"\b(ppi_(?:gpu|batch|csv)_\w+)\s*\(", text)))
+
+
+def read_csv(path):
+    """PPI's training CSV read by the library's reader (ppi_csv_read, the
+    rules of src/main.cc:32-122): a row-major nlin x ncol float32 array;
+    raises PpiGpuError with the reader's message for a file it rejects."""
+    L = load_library()
+    nlin = np.zeros(1, np.int32)
+    ncol = np.zeros(1, np.int32)
+    msg = C.create_string_buffer(512)
+    p = os.fsencode(path)
+    st = L.ppi_csv_read(p, None, 0, 0, _i(nlin), _i(ncol), msg, 512)
+    if st != 0:
+        raise PpiGpuError(st, msg.value.decode())
+    cm = np.zeros((int(ncol[0]), max(1, int(nlin[0]))), np.float32)
+    st = L.ppi_csv_read(p, _f(cm), cm.size, cm.shape[1], _i(nlin), _i(ncol), msg, 512)
+    if st != 0:
+        raise PpiGpuError(st, msg.value.decode())
+    return np.ascontiguousarray(cm[:, :int(nlin[0])].T)
 
 
 def _f(a):
@@ -193,6 +215,14 @@ class Evaluator:
         nlin, ncol = self._rows.shape
         self._check(self._L.ppi_gpu_set_dataset_rowmajor(self._h, _f(self._rows), nlin, ncol))
         self.nlin = nlin
+
+    def set_dataset_csv(self, path):
+        """PPI's training CSV straight to the device (ppi_gpu_set_dataset_csv)."""
+        nlin = np.zeros(1, np.int32)
+        ncol = np.zeros(1, np.int32)
+        self._check(self._L.ppi_gpu_set_dataset_csv(self._h, os.fsencode(path), _i(nlin), _i(ncol)))
+        self.nlin = int(nlin[0])
+        return int(nlin[0]), int(ncol[0])
 
     def evaluate(self, phenotype, ephemeral, size, alpha=0.0):
         ph = np.ascontiguousarray(phenotype, np.int32)

@@ -61,6 +61,23 @@ def build(verbose=False, ptxas_verbose=False) -> str:
     return LIB
 
 
+# The benchmark's measurement library: per-opcode arithmetic throughput for
+# the op-mix-aware roofline (not part of the evaluator library).
+OPCOST_SRC = os.path.join(PKG, "bench_csrc", "opcost.cu")
+OPCOST_LIB = os.path.join(OUT, "libppi_opcost.so")
+
+
+def build_opcost() -> str:
+    os.makedirs(OUT, exist_ok=True)
+    tmp = OPCOST_LIB + ".tmp"
+    cmd = [nvcc(), "-shared", OPCOST_SRC, "-o", tmp] + ARCH + NVCC_FLAGS + ["-cudart", "shared"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("nvcc failed for %s:\n%s\n%s" % (OPCOST_SRC, r.stdout, r.stderr))
+    os.replace(tmp, OPCOST_LIB)
+    return OPCOST_LIB
+
+
 if __name__ == "__main__":
     import sys
     print(build(verbose=True, ptxas_verbose="-v" in sys.argv))

@@ -59,6 +59,56 @@ def test_evolution_mode(gpu_lib, oracle_lib, tmp_path, name, strategy, lanes):
         assert "gpops_kernel" in stdout and "Device: CUDA" in stdout
 
 
+def _write_csv(path, rows, header=True):
+    """rows as PPI's CSV: '%.9g' round-trips every float32 exactly."""
+    with open(path, "w") as f:
+        if header:
+            f.write(",".join("x%d" % k for k in range(rows.shape[1] - 1)) + ",y\n")
+        f.write("# written by the test\n")
+        for r in rows:
+            f.write(",".join("%.9g" % v for v in r) + "\n")
+
+
+@pytest.mark.parametrize("name,strategy,lanes", [("cfg2", "PDP", 64), ("cfg5", "DP", 40)])
+def test_dataset_read_from_the_csv_file(gpu_lib, oracle_lib, tmp_path, name, strategy, lanes):
+    """With PPI's -d flag on the command line the adapter uploads the dataset
+    straight from that file (ppi_gpu_set_dataset_csv) instead of main.cc's
+    float** rows; the results are the same."""
+    d = load_golden(name)
+    exe = _driver(d, tmp_path)
+    csv = str(tmp_path / "data.csv")
+    _write_csv(csv, d["rows"])
+    gens = [(d["phenotype"], d["ephemeral"], d["size"])]
+    out, stdout = run_driver(exe, 0, d["rows"], gens, float(d["alpha"]),
+                             _flags(strategy, lanes) + ["-d", csv], env={"PPI_GPU_MATH": "parity"})
+    assert "read from the CSV file" in stdout
+    o = oracle_for(oracle_lib, d)
+    ref = o.evaluate(*gens[0], strategy, lanes, float(d["alpha"]))
+    assert_bitexact(out[0][0], ref, "%s from CSV" % name)
+    assert out[0][1] == expected_best(oracle_lib, o, *gens[0], strategy, lanes, float(d["alpha"]))
+
+
+def test_csv_entry_point_equals_row_upload(gpu_lib, tmp_path):
+    d = load_golden("random")
+    csv = str(tmp_path / "random.csv")
+    _write_csv(csv, d["rows"], header=False)
+    import ppi_gpu
+    evs = []
+    for how in ("csv", "rows"):
+        ev = ppi_gpu.Evaluator(d["symtab"], d["max_size"], len(d["size"]), "PDP", 0, d["ef"],
+                               d["cost_or_none"], bool(d["reduce_max"]), bool(d["protected"]),
+                               "parity")
+        if how == "csv":
+            assert ev.set_dataset_csv(csv) == d["rows"].shape
+        else:
+            ev.set_dataset(d["rows"])
+        evs.append(ev.evaluate(d["phenotype"], d["ephemeral"], d["size"], 1e-6))
+    assert_bitexact(evs[0][0], evs[1][0], "csv vs rows")
+    assert evs[0][1] == evs[1][1]
+    with pytest.raises(ppi_gpu.PpiGpuError, match="Failed to open dataset file"):
+        ev.set_dataset_csv(str(tmp_path / "absent.csv"))
+
+
 @pytest.mark.parametrize("name,strategy,lanes", CASES[:4])
 def test_ppp_modes(gpu_lib, oracle_lib, tmp_path, name, strategy, lanes):
     d = load_golden(name)
