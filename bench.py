@@ -162,12 +162,21 @@ def cpu_sample(wl, ph, eph, sz, budget_s, threads=0, chunk=0, alpha=1e-6):
     return ops / t / 1e9, done, cores, t, np.concatenate(fits)
 
 
-def batch_cpu_sample(pops, sym, fraction, threads=0, slice_index=0):
+def pop_oracle(p, sym, threads=0):
+    """The oracle over one population's dataset and settings."""
+    from oracle import pyoracle
+    return pyoracle.Oracle(p["rows"], sym, p["error_fn"], None, bool(p.get("reduce_max", False)),
+                           p["protected"], False, threads)
+
+
+def batch_cpu_sample(pops, sym, fraction, threads=0, slice_index=0, sm_count=152):
     """Oracle port on a slice of every population's programs (a `fraction` of
     each, and at least one per core: the port runs programs in parallel; slice
-    `slice_index` of the population, wrapping), all records:
+    `slice_index` of the population, wrapping), all records, in each
+    population's strategy and lane count:
     (GPop/s, programs, cores, seconds, [(population, slice, fitness)])."""
     from oracle import pyoracle
+    from ppi_gpu import workloads
     pyoracle.build()
     cores = threads if threads > 0 else (os.cpu_count() or 1)
     ops, t, done, fits = 0, 0.0, 0, []
@@ -175,10 +184,11 @@ def batch_cpu_sample(pops, sym, fraction, threads=0, slice_index=0):
         k = min(p["n"], max(cores, int(round(p["n"] * fraction))))
         lo = (slice_index * k) % max(1, p["n"] - k + 1)
         sl = slice(lo, lo + k)
-        o = pyoracle.Oracle(p["rows"], sym, p["error_fn"], None, False, p["protected"], False, threads)
-        lanes = min(p["rows"].shape[0], 1024)
+        o = pop_oracle(p, sym, threads)
+        strategy = p.get("strategy", "PDP")
+        lanes = workloads.default_lanes(strategy, p["rows"].shape[0], sm_count)
         t0 = time.perf_counter()
-        f = o.evaluate(p["phenotype"][sl], p["ephemeral"][sl], p["size"][sl], "PDP", lanes, 0.0)
+        f = o.evaluate(p["phenotype"][sl], p["ephemeral"][sl], p["size"][sl], strategy, lanes, 0.0)
         t += time.perf_counter() - t0
         fits.append((i, sl, f))
         ops += int(p["size"][sl].astype(np.int64).sum()) * p["rows"].shape[0]
@@ -253,7 +263,7 @@ def opmix_roofline(achieved, prog_sets):
                    "whole GPU (libppi_opcost.so); terminals free"}
 
 
-def parity_block(gpu, ref, gpu64=None, fp64=None, what=""):
+def parity_block(gpu, ref, gpu64=None, fp64=None, what="", ref64=None):
     """Fitness of the timed GPU path against the oracle on the same programs
     (the reference's sequential arithmetic in the same strategy's order: only
     the transcendental functions' rounding differs in fast math), and against
@@ -273,30 +283,42 @@ def parity_block(gpu, ref, gpu64=None, fp64=None, what=""):
            "median_rel_diff": float(np.median(rel)) if rel.size else 0.0,
            "frac_within_1e-5": round(float((rel <= 1e-5).mean()), 5) if rel.size else 1.0}
     if fp64 is not None:
-        g = np.asarray(gpu64, np.float64)
         f = np.asarray(fp64, np.float64)
-        ok = (g < 1e30) & np.isfinite(f)
-        r64 = np.abs(g[ok] - f[ok]) / np.maximum(np.abs(f[ok]), 1e-300)
-        out["fp64"] = {"programs": int(len(f)),
-                       "sentinel_agreement": round(float(((g >= 1e30) == ~np.isfinite(f)).mean()), 5),
-                       "max_rel_err": float(r64.max()) if r64.size else 0.0,
-                       "median_rel_err": float(np.median(r64)) if r64.size else 0.0,
-                       "frac_within_1e-5": round(float((r64 <= 1e-5).mean()), 5) if r64.size else 1.0}
+
+        def against_fp64(vals):
+            g = np.asarray(vals, np.float64)
+            ok = (g < 1e30) & np.isfinite(f)
+            r64 = np.abs(g[ok] - f[ok]) / np.maximum(np.abs(f[ok]), 1e-300)
+            return {"sentinel_agreement": round(float(((g >= 1e30) == ~np.isfinite(f)).mean()), 5),
+                    "max_rel_err": float(r64.max()) if r64.size else 0.0,
+                    "median_rel_err": float(np.median(r64)) if r64.size else 0.0,
+                    "frac_within_1e-5": round(float((r64 <= 1e-5).mean()), 5) if r64.size else 1.0}
+        # the same programs' reference float fitness against FP64: how far
+        # float evaluation itself is from FP64 on them
+        out["fp64"] = dict(against_fp64(gpu64), programs=int(len(f)),
+                           reference_float=against_fp64(ref[:len(f)] if ref64 is None else ref64))
     return out
 
 
 def batch_config(pops, work, extra):
     nprog = sum(p["n"] for p in pops)
-    return dict({"workload": "uneven-batch-%dpops" % len(pops), "populations": len(pops),
-                 "programs": int(nprog),
+    mixed = len({(p["strategy"], p["error_fn"], bool(p.get("reduce_max", False))) for p in pops}) > 1
+
+    def count(key, v):
+        return sum(1 for p in pops if p.get(key) == v)
+    settings = ({"strategy": {s: count("strategy", s) for s in ("PP", "DP", "PDP")},
+                 "error_fn": {e: count("error_fn", e) for e in ("abs", "squared")},
+                 "reduce_max": sum(1 for p in pops if p.get("reduce_max"))}
+                if mixed else {"strategy": "PDP", "error_fn": "abs", "reduce_max": False})
+    return dict({"workload": "uneven-batch-%dpops%s" % (len(pops), "-mixed" if mixed else ""),
+                 "populations": len(pops), "programs": int(nprog),
                  "records": [int(min(p["rows"].shape[0] for p in pops)),
                              int(max(p["rows"].shape[0] for p in pops))],
                  "features": [int(min(p["rows"].shape[1] - 1 for p in pops)),
                               int(max(p["rows"].shape[1] - 1 for p in pops))],
                  "max_size": 256, "mean_size": round(float(np.mean(np.concatenate(
                      [p["size"] for p in pops]))), 2),
-                 "strategy": "PDP", "error_fn": "abs", "reduce_max": False, "protected": True,
-                 "ops_per_step": int(work)}, **extra)
+                 "protected": True, "ops_per_step": int(work)}, **settings, **extra)
 
 
 def run_reference(args):
@@ -390,11 +412,12 @@ def run_batch(args):
     from ppi_gpu import workloads
     rank, world, local = dist_env()
     torch.cuda.set_device(local)
-    if world > 1:
+    if world > 1 and not torch.distributed.is_initialized():
         import torch.distributed as dist
         dist.init_process_group("nccl")
     g, pops = workloads.uneven_batch(seed=11 + rank, n_pops=args.populations,
-                                     pop_range=(256, args.max_programs))
+                                     pop_range=(256, args.max_programs),
+                                     mixed=getattr(args, "mixed", False))
     sym = g.symbol_table_arrays()
     ph = np.concatenate([p["phenotype"] for p in pops])
     eph = np.concatenate([p["ephemeral"] for p in pops])
@@ -453,8 +476,8 @@ def run_batch(args):
     # plain: one evaluator per population, launched back to back
     plain_evs, offs, begin = [], [], 0
     for p in pops:
-        e = ppi_gpu.Evaluator(sym, 256, p["n"], "PDP", 0, "abs", None, False, True, args.math,
-                              device=local)
+        e = ppi_gpu.Evaluator(sym, 256, p["n"], p["strategy"], 0, p["error_fn"], None,
+                              bool(p.get("reduce_max", False)), True, args.math, device=local)
         e.set_dataset(p["rows"])
         plain_evs.append(e)
         offs.append(begin)
@@ -507,7 +530,8 @@ def run_batch(args):
     peak = sm_count * 128 * max_mhz * 1e6 / 1e9          # FP32 lane-ops/s, in G
     block, grid, rows, tune = be.shape()
     kernel_ms = float(np.mean(step_ms))
-    cpu_v, cpu_n, cpu_cores, cpu_t, cpu_fits = batch_cpu_sample(pops, sym, args.cpu_fraction)
+    cpu_v, cpu_n, cpu_cores, cpu_t, cpu_fits = batch_cpu_sample(pops, sym, args.cpu_fraction,
+                                                                sm_count=sm_count)
     parity = batch_parity(pops, sym, fit_b, cpu_fits, offs)
     issue = profile_value("eval_batch_kernel_uneven-batch-mid", "issue_active_frac")
     line = {
@@ -562,19 +586,21 @@ def batch_parity(pops, sym, fit_gpu, cpu_fits, offs, fp64_per_pop=2):
     against the oracle's, and of its first programs per population against
     an FP64 re-evaluation."""
     from oracle import pyoracle
-    gpu, ref, g64, f64 = [], [], [], []
+    gpu, ref, g64, f64, r64 = [], [], [], [], []
     for i, sl, f in cpu_fits:
         p = pops[i]
         gsl = fit_gpu[offs[i] + sl.start: offs[i] + sl.stop]
         gpu.append(gsl)
         ref.append(f)
         k = min(fp64_per_pop, sl.stop - sl.start)
-        o = pyoracle.Oracle(p["rows"], sym, p["error_fn"], None, False, p["protected"], False)
+        o = pop_oracle(p, sym)
         sub = slice(sl.start, sl.start + k)
         f64.append(o.evaluate64(p["phenotype"][sub], p["ephemeral"][sub], p["size"][sub]))
         g64.append(gsl[:k])
+        r64.append(f[:k])
     return parity_block(np.concatenate(gpu), np.concatenate(ref), np.concatenate(g64),
-                        np.concatenate(f64), ", PDP over each population's 1024 lanes")
+                        np.concatenate(f64), ", each population in its own strategy and lanes",
+                        np.concatenate(r64))
 
 
 def run_adjoint(args):
@@ -806,7 +832,11 @@ def run_polynomial(args):
 SUB_CONFIGS = [("iris", "iris", 1000, 150, 5, 3.0),
                ("polynomial", "polynomial", 30_000, 100_000, 5, 5.0),
                ("stream", "stream", 30_000, 4_000_000, 2, 5.0),
-               ("adjoint", "adjoint", 10_000, 100_000, 5, 0.0)]
+               ("adjoint", "adjoint", 10_000, 100_000, 5, 0.0),
+               # the uneven batch with each population's strategy (PP / DP /
+               # PDP), error function and reduction drawn at random: batched
+               # vs plain at identical fitness over mixed settings
+               ("uneven_mixed", "uneven-mixed", 0, 0, 3, 0.005)]
 
 
 def sub_line(line):
@@ -819,10 +849,14 @@ def run_sub_configs(args):
     out = {}
     for key, workload, population, records, steps, cpu_s in SUB_CONFIGS:
         a = argparse.Namespace(**vars(args))
-        a.workload, a.population, a.records = workload, population, records
-        a.steps, a.cpu_seconds = min(args.steps, steps), cpu_s
+        a.workload, a.steps = workload, min(args.steps, steps)
         t0 = time.perf_counter()
-        line = run_adjoint(a) if workload == "adjoint" else run_polynomial(a)
+        if workload == "uneven-mixed":
+            a.mixed, a.cpu_fraction = True, cpu_s
+            line = run_batch(a)
+        else:
+            a.population, a.records, a.cpu_seconds = population, records, cpu_s
+            line = run_adjoint(a) if workload == "adjoint" else run_polynomial(a)
         sub = sub_line(line)
         sub["wall_s"] = round(time.perf_counter() - t0, 1)
         out[key] = sub

@@ -157,6 +157,45 @@ __device__ __forceinline__ void adj_trig_case(const float (&g)[R], float (&x)[R]
    for (int r = 0; r < R; ++r) d0[r] = OP == PPI_OP_SIN ? g[r] * x[r] : -(g[r] * x[r]);
 }
 
+// The quotient g / a of the division and logarithm cases, rolled the same
+// way (numerators and denominators rotate through one inlined IEEE
+// division): the same quotients as the unrolled form, a fraction of its code.
+constexpr bool kAdjRollQuotient = true;
+template <int R>
+__device__ __forceinline__ void adj_quotients(const float (&g)[R], const float (&a)[R], float (&q)[R]) {
+   float d[R];
+#pragma unroll
+   for (int r = 0; r < R; ++r) { q[r] = g[r]; d[r] = a[r]; }
+#pragma unroll 1
+   for (int r = 0; r < R; ++r) {
+      const float t = q[0] / d[0];
+#pragma unroll
+      for (int k = 0; k < R - 1; ++k) { q[k] = q[k + 1]; d[k] = d[k + 1]; }
+      q[R - 1] = t;
+   }
+}
+
+// Division and logarithm partials from the rolled quotients, as adj_bp
+// forms them.
+template <int OP, int R>
+__device__ __forceinline__ void adj_quotient_case(const float (&g)[R], const float (&x)[R], const float (&y)[R],
+                                                  const float (&v)[R], int prot, float (&d0)[R], float (&d1)[R]) {
+   const float kLn2 = 0.693147180559945309f, kLn10 = 2.30258509299404568f;
+   float q[R];
+   if constexpr (OP == PPI_OP_DIV) adj_quotients(g, y, q);
+   else adj_quotients(g, x, q);
+#pragma unroll
+   for (int r = 0; r < R; ++r) {
+      d0[r] = 0.0f;
+      d1[r] = 0.0f;
+      if constexpr (OP == PPI_OP_DIV) {
+         if (!(prot && y[r] == 0.0f)) { d0[r] = q[r]; d1[r] = -(q[r] * v[r]); }
+      } else if (!(prot && x[r] < 1.0f)) {
+         d0[r] = OP == PPI_OP_LOG ? q[r] : (OP == PPI_OP_LOG2 ? q[r] / kLn2 : q[r] / kLn10);
+      }
+   }
+}
+
 #define ADJ_REV_CASE(OP)                                                                  \
    case OP:                                                                               \
       if constexpr (adj_reads_a(OP)) adj_operand(i0.y & 0xFFFFu, mine, T, P, tab, x);      \
@@ -165,6 +204,11 @@ __device__ __forceinline__ void adj_trig_case(const float (&g)[R], float (&x)[R]
       if constexpr (kAdjRollTrig && (OP == PPI_OP_SIN || OP == PPI_OP_COS)) {              \
          adj_trig_case<OP, R>(g, x, d0);                                                   \
          _Pragma("unroll") for (int r = 0; r < R; ++r) { d1[r] = 0.0f; d2[r] = 0.0f; }     \
+      } else if constexpr (kAdjRollQuotient &&                                             \
+                           (OP == PPI_OP_DIV || OP == PPI_OP_LOG || OP == PPI_OP_LOG2 ||    \
+                            OP == PPI_OP_LOG10)) {                                         \
+         adj_quotient_case<OP, R>(g, x, y, v, prot, d0, d1);                               \
+         _Pragma("unroll") for (int r = 0; r < R; ++r) d2[r] = 0.0f;                       \
       } else {                                                                             \
          _Pragma("unroll") for (int r = 0; r < R; ++r)                                    \
             adj_bp<OP>(g[r], x[r], y[r], 0.0f, v[r], prot, d0[r], d1[r], d2[r]);          \

@@ -86,6 +86,7 @@ struct BatchGeo {
    size_t smem_wide = 0;
    bool wide = false;
    int wide_kernel = 1;                // 2: every population PP or PDP (whole-quad direct reads)
+   int main_kernel = 0;                // kMainHi: the main pass's 64-register build
 };
 
 struct ppi_batch {
@@ -200,10 +201,15 @@ ppi_status batch_geometry(ppi_batch* b, int P, int rows_req, BatchGeo* g) {
          return 0;
       return per_sm;
    };
+   // the main pass's kernel at a row count: the 64-register build where it
+   // lets more CTAs fit than the 80-register one
+   auto main_kernel_for = [&](int rows) { return occupancy(kMainHi, rows) > occupancy(0, rows) ? kMainHi : 0; };
+   auto occ_main = [&](int rows) { return occupancy(main_kernel_for(rows), rows); };
    auto best_rows = [&](int direct) {
-      const int top = occupancy(direct, 1);
+      auto occ = [&](int r) { return direct == 0 ? occ_main(r) : occupancy(direct, r); };
+      const int top = occ(1);
       int rows = 1;
-      while (rows < fit && occupancy(direct, rows + 1) >= top) ++rows;
+      while (rows < fit && occ(rows + 1) >= top) ++rows;
       return rows;
    };
    // whole-quad direct reads need every tile to start on a multiple of 4
@@ -220,7 +226,8 @@ ppi_status batch_geometry(ppi_batch* b, int P, int rows_req, BatchGeo* g) {
    g->fit = fit;
    g->rows = rows;
    g->smem = smem_for(rows);
-   g->per_sm = occupancy(0, rows);
+   g->main_kernel = main_kernel_for(rows);
+   g->per_sm = occupancy(g->main_kernel, rows);
    if (g->per_sm < 1) return bfail(b, PPI_ERR_UNSUPPORTED, "tile does not fit on an SM");
    g->grid = std::max(1, std::min(b->total, g->per_sm * b->sm_count));
    g->rows_wide = rows2;
@@ -254,7 +261,7 @@ ppi_status enqueue_step(ppi_batch* b, const int32_t* ph, const float* eph, const
    a.fitness = fit; a.pop_key = b->d_pop_key; a.pop_done = b->d_pop_done; a.best_index = best;
    a.stats = b->d_stats; a.n_main = b->d_n_main; a.status = b->d_status;
    a.rows = g.rows; a.wide_pass = 0;
-   PPI_BCUDA(b, launch_evaluate_batch(b->math, b->opset, 0, a, g.block, g.grid, g.smem, s));
+   PPI_BCUDA(b, launch_evaluate_batch(b->math, b->opset, g.main_kernel, a, g.block, g.grid, g.smem, s));
    b->last_launches = 4;   // translate, order scan, order scatter, main pass
    if (g.wide) {
       a.rows = g.rows_wide; a.wide_pass = 1;

@@ -178,18 +178,30 @@ const char* plan_geometry(int strategy, int lanes, int math, int opset, int nlin
    };
    // main pass: programs whose columns all fit, lean kernel; when the whole
    // population is resident in one wave at a larger tile, the larger tile
-   // (the most rows at which it still is: occupancy falls as rows grow)
-   int rows = best_rows(0);
-   if ((long long)occupancy(0, fit) * sm_count >= n_max) {
-      rows = fit;
-   } else if ((long long)occupancy(0, rows + 1) * sm_count >= n_max && rows < fit) {
-      int lo = rows + 1, hi = fit;   // occupancy(lo) fits, occupancy(hi) does not
-      while (hi - lo > 1) {
-         const int mid = (lo + hi) / 2;
-         if ((long long)occupancy(0, mid) * sm_count >= n_max) lo = mid;
-         else hi = mid;
+   // (the most rows at which it still is: occupancy falls as rows grow).
+   // Planned with each register bound of the main-pass kernel; the one with
+   // more resident CTAs at its rows runs (the 64-register build only where
+   // its tile lets more CTAs fit).
+   auto main_rows = [&](int k) {
+      int r = best_rows(k);
+      if ((long long)occupancy(k, fit) * sm_count >= n_max) {
+         r = fit;
+      } else if ((long long)occupancy(k, r + 1) * sm_count >= n_max && r < fit) {
+         int lo = r + 1, hi = fit;   // occupancy(lo) fits, occupancy(hi) does not
+         while (hi - lo > 1) {
+            const int mid = (lo + hi) / 2;
+            if ((long long)occupancy(k, mid) * sm_count >= n_max) lo = mid;
+            else hi = mid;
+         }
+         r = lo;
       }
-      rows = lo;
+      return r;
+   };
+   int main_kernel = 0, rows = main_rows(0);
+   const int rows_hi = main_rows(kMainHi);
+   if (occupancy(kMainHi, rows_hi) > occupancy(0, rows)) {
+      main_kernel = kMainHi;
+      rows = rows_hi;
    }
    // second pass: the rest, with the columns that do not fit read directly
    // (room at least for the deepest slot need and the target)
@@ -206,7 +218,8 @@ const char* plan_geometry(int strategy, int lanes, int math, int opset, int nlin
    g->aligned = aligned;
    g->rows = rows;
    g->smem = evaluate_smem_bytes(code_stride, rows, P, R, L, aligned);
-   g->per_sm[0] = occupancy(0, rows);
+   g->per_sm[0] = occupancy(main_kernel, rows);
+   g->main_kernel = main_kernel;
    if (g->per_sm[0] < 1) return "evaluator does not fit on an SM";
    g->grid = std::max(1, std::min(n_max, g->per_sm[0] * sm_count));
    g->wide = rows < rows_max;

@@ -26,7 +26,7 @@ cudaError_t evaluate_batch_occupancy_fast(int opset, int direct, int block, size
 
 extern "C" int32_t ppi_gpu_kernel_arch(void) {
    cudaFuncAttributes fa{};
-   if (cudaFuncGetAttributes(&fa, ppi::ev::eval_kernel<ppi::kMathFast, ppi::kR, ppi::kOpsetArith, 0>) !=
+   if (cudaFuncGetAttributes(&fa, ppi::ev::eval_kernel<ppi::kMathFast, ppi::kR, ppi::kOpsetArith, 0, 0>) !=
        cudaSuccess)
       return -1;
    return fa.binaryVersion;

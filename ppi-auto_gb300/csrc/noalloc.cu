@@ -235,7 +235,8 @@ extern "C" ppi_status ppi_gpu_evaluate_noalloc(const ppi_gpu_config* c, const fl
    if (cudaMemsetAsync(stats, 0, sizeof(DevStats), s) != cudaSuccess) return PPI_ERR_CUDA;
    if (launch_translate(c->math, t, s) != cudaSuccess) return PPI_ERR_CUDA;
    e.rows = g.rows; e.wide_pass = 0; e.final_pass = g.wide ? 0 : 1;
-   if (launch_evaluate(c->math, g.opset, 0, e, g.block, g.grid, g.smem, s) != cudaSuccess) return PPI_ERR_CUDA;
+   if (launch_evaluate(c->math, g.opset, g.main_kernel, e, g.block, g.grid, g.smem, s) != cudaSuccess)
+      return PPI_ERR_CUDA;
    if (g.wide) {
       e.rows = g.rows_wide; e.wide_pass = 1; e.final_pass = 1;
       if (launch_evaluate(c->math, g.opset, g.wide_kernel, e, g.block, g.grid_wide, g.smem_wide, s) != cudaSuccess)

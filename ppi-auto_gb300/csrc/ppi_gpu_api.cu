@@ -210,7 +210,7 @@ ppi_status enqueue(ppi_gpu* h, const int32_t* d_ph, const float* d_eph, const in
    h->last_n = n;
    PPI_CUDA(h, cudaEventRecord(h->evm, s));
    e.rows = g.rows; e.wide_pass = 0; e.final_pass = g.wide ? 0 : 1;
-   PPI_CUDA(h, launch_evaluate(h->cfg.math, g.opset, 0, e, g.block, std::min(g.grid, n), g.smem, s));
+   PPI_CUDA(h, launch_evaluate(h->cfg.math, g.opset, g.main_kernel, e, g.block, std::min(g.grid, n), g.smem, s));
    h->last_launches = 2;
    if (g.wide) {
       e.rows = g.rows_wide; e.wide_pass = 1; e.final_pass = 1;

@@ -181,13 +181,18 @@ def _random_target(rng, X, depth=5):
 
 
 def uneven_batch(seed=11, n_pops=64, pop_range=(256, 30000), rec_range=(100, 1_000_000),
-                 feat_range=(1, 32), mean_len=40, len_range=(4, 256), max_size=256):
+                 feat_range=(1, 32), mean_len=40, len_range=(4, 256), max_size=256, mixed=False):
     """Uneven batch: n_pops populations with log-uniform sizes and record
     counts, 1-32 N(0,1) features, targets from a random depth-5 expression +
     N(0, 0.05) noise, and programs of geometric length (mean 40, 4..256)
     generated as random valid prefix trees.  Returns (grammar, list of
-    population dicts with rows / n / phenotype / ephemeral / size)."""
+    population dicts with rows / n / phenotype / ephemeral / size).  Every
+    population is PDP with the absolute error and the sum; with mixed=True
+    each draws its strategy (PP, DP, PDP), error function (absolute or
+    squared) and reduction (REDUCEMAX one time in four) instead, from a
+    generator of its own, so the programs and datasets stay the same."""
     rng = np.random.default_rng(seed)
+    mix = np.random.default_rng(seed + 7919)
     g = G.load(os.path.join(GRAMMARS, "config2_poly.bnf"))
     pops = []
     for p in range(n_pops):
@@ -203,10 +208,24 @@ def uneven_batch(seed=11, n_pops=64, pop_range=(256, 30000), rec_range=(100, 1_0
         epf = np.zeros((n, max_size), np.float32)
         phf[:, :ph.shape[1]] = ph
         epf[:, :ep.shape[1]] = ep
-        pops.append(dict(rows=rows, n=n, phenotype=phf, ephemeral=epf,
-                         size=lengths.astype(np.int32), strategy="PDP", error_fn="abs",
-                         protected=True))
+        pop = dict(rows=rows, n=n, phenotype=phf, ephemeral=epf, size=lengths.astype(np.int32),
+                   strategy="PDP", error_fn="abs", protected=True, reduce_max=False)
+        if mixed:
+            pop["strategy"] = ("PP", "DP", "PDP")[int(mix.integers(3))]
+            pop["error_fn"] = ("abs", "squared")[int(mix.integers(2))]
+            pop["reduce_max"] = bool(mix.random() < 0.25)
+        pops.append(pop)
     return g, pops
+
+
+def default_lanes(strategy, nlin, sm_count=152):
+    """The lane count ppi_gpu_set_dataset picks when none is given (the
+    reference's rule, accelerator.cc:296-330, on a device of sm_count units)."""
+    if strategy == "PP":
+        return 1
+    if strategy == "PDP":
+        return min(nlin, 1024)
+    return min(1024, -(-nlin // sm_count))
 
 
 def adjoint(seed=21, nlin=100_000, population=10_000, max_size=64, mean_len=20):
