@@ -136,8 +136,10 @@ def profile_value(name, key):
 
 
 def profile_traffic(workload):
-    """Per-step DRAM bytes of the evaluator kernels from a committed ncu summary."""
-    return profile_value("eval_kernel_" + workload, "traffic_bytes_per_launch")
+    """DRAM bytes (read + written) of one step's kernels from a committed ncu
+    summary: the launch list of that workload, else its kernel profile."""
+    v = profile_value("launches_" + workload, "traffic_bytes_per_step")
+    return v if v is not None else profile_value("eval_kernel_" + workload, "traffic_bytes_per_launch")
 
 
 def cpu_sample(wl, ph, eph, sz, budget_s, threads=0, chunk=0, alpha=1e-6):
@@ -533,7 +535,16 @@ def run_batch(args):
     cpu_v, cpu_n, cpu_cores, cpu_t, cpu_fits = batch_cpu_sample(pops, sym, args.cpu_fraction,
                                                                 sm_count=sm_count)
     parity = batch_parity(pops, sym, fit_b, cpu_fits, offs)
-    issue = profile_value("eval_batch_kernel_uneven-batch-mid", "issue_active_frac")
+    # issue activity of the evaluator kernels over one step of this same
+    # configuration (launch-list capture), else of the mid-size profile
+    issue = profile_value("launches_uneven-batch", "issue_active_frac")
+    if issue is None:
+        issue = profile_value("eval_batch_kernel_uneven-batch-mid", "issue_active_frac")
+    traffic = profile_traffic("uneven-batch")
+    # bytes a step must move at least: every dataset once, the programs in,
+    # the fitness and best indices out
+    algorithmic = int(sum(p["rows"].nbytes for p in pops) + ph.nbytes + eph.nbytes + sz.nbytes +
+                      n * 4 + len(pops) * 4)
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup,
@@ -565,7 +576,10 @@ def run_batch(args):
                                                    (sm_count * 128 * clk["sm_mhz"] / 1e3), 4)
                      if clk.get("sm_mhz") else None,
                      "issue_active_frac": issue,
-                     "traffic": profile_traffic("uneven-batch"),
+                     "traffic": traffic,
+                     "traffic_unit": "bytes per step (DRAM read + write, ncu)",
+                     "algorithmic_bytes": algorithmic,
+                     "traffic_over_algorithmic": round(traffic / algorithmic, 2) if traffic else None,
                      "opmix": opmix_roofline(all_ops / world / (kernel_ms / 1e3) / 1e9,
                                              [(p["phenotype"], p["size"], p["rows"].shape[0], sym)
                                               for p in pops])},

@@ -87,6 +87,7 @@ struct BatchGeo {
    bool wide = false;
    int wide_kernel = 1;                // 2: every population PP or PDP (whole-quad direct reads)
    int main_kernel = 0;                // kMainHi: the main pass's 64-register build
+                                       //   (both + kOneLane when a population has one lane)
 };
 
 struct ppi_batch {
@@ -195,9 +196,14 @@ ppi_status batch_geometry(ppi_batch* b, int P, int rows_req, BatchGeo* g) {
    if (fixed + T * 4 > kSmemCap) return bfail(b, PPI_ERR_UNSUPPORTED, "tile does not fit in shared memory");
    const int rows_max = max_program_rows(b->max_ncol);
    const int fit = (int)std::min<size_t>(rows_max, (kSmemCap - fixed) / (T * 4));
+   // a population with one lane (PP, or PDP over one lane): the kernels
+   // with the one-lane chain run the whole batch
+   int one = 0;
+   for (const PopDesc& p : b->host_pops)
+      if (p.strategy != PPI_STRATEGY_DP && p.lanes == 1) one = kOneLane;
    auto occupancy = [&](int direct, int rows) {
       int per_sm = 0;
-      if (evaluate_batch_occupancy(b->math, b->opset, direct, P, smem_for(rows), &per_sm) != cudaSuccess)
+      if (evaluate_batch_occupancy(b->math, b->opset, direct | one, P, smem_for(rows), &per_sm) != cudaSuccess)
          return 0;
       return per_sm;
    };
@@ -228,13 +234,14 @@ ppi_status batch_geometry(ppi_batch* b, int P, int rows_req, BatchGeo* g) {
    g->smem = smem_for(rows);
    g->main_kernel = main_kernel_for(rows);
    g->per_sm = occupancy(g->main_kernel, rows);
+   g->main_kernel |= one;
    if (g->per_sm < 1) return bfail(b, PPI_ERR_UNSUPPORTED, "tile does not fit on an SM");
    g->grid = std::max(1, std::min(b->total, g->per_sm * b->sm_count));
    g->rows_wide = rows2;
    g->smem_wide = smem_for(rows2);
    g->grid_wide = std::max(1, std::min(b->total, std::max(1, occupancy(wk, rows2)) * b->sm_count));
    g->wide = rows < rows_max;
-   g->wide_kernel = wk;
+   g->wide_kernel = wk | one;
    return PPI_OK;
 }
 

@@ -1,5 +1,6 @@
 // evaluate.cu -- launch geometry and math-mode dispatch of the evaluator
-// kernels (evaluate_impl.cuh, instantiated in evaluate_{fast,parity,native}.cu).
+// kernels (evaluate_impl.cuh, instantiated in evaluate_{fast,parity,native}.cu
+// and, with the one-lane chain, evaluate_{fast,parity,native}_lane1.cu).
 #include <algorithm>
 #include <cmath>
 #include <cstdlib>
@@ -8,27 +9,25 @@
 
 namespace ppi {
 
-cudaError_t launch_evaluate_fast(int opset, int direct, const EvalArgs& a, int block, int grid, size_t smem,
-                              cudaStream_t s);
+// Entry points of evaluate_<math>.cu (suffix <math>) and evaluate_<math>_lane1.cu
+// (suffix <math>1).
+#define PPI_DECLARE_ENTRY_POINTS(S)                                                             \
+   cudaError_t launch_evaluate_##S(int opset, int direct, const EvalArgs& a, int block, int grid, \
+                                   size_t smem, cudaStream_t s);                              \
+   cudaError_t launch_evaluate_batch_##S(int opset, int direct, const BatchArgs& a, int block,  \
+                                         int grid, size_t smem, cudaStream_t s);              \
+   cudaError_t evaluate_occupancy_##S(int opset, int direct, int block, size_t smem, int* per_sm); \
+   cudaError_t evaluate_batch_occupancy_##S(int opset, int direct, int block, size_t smem, int* per_sm);
+PPI_DECLARE_ENTRY_POINTS(fast)
+PPI_DECLARE_ENTRY_POINTS(fast1)
+PPI_DECLARE_ENTRY_POINTS(parity)
+PPI_DECLARE_ENTRY_POINTS(parity1)
+PPI_DECLARE_ENTRY_POINTS(native)
+PPI_DECLARE_ENTRY_POINTS(native1)
+#undef PPI_DECLARE_ENTRY_POINTS
 cudaError_t launch_predict_fast(int opset, const PredictArgs& a, int block, int grid, size_t smem, cudaStream_t s);
-cudaError_t launch_evaluate_batch_fast(int opset, int direct, const BatchArgs& a, int block, int grid,
-                                    size_t smem, cudaStream_t s);
-cudaError_t evaluate_occupancy_fast(int opset, int direct, int block, size_t smem, int* per_sm);
-cudaError_t evaluate_batch_occupancy_fast(int opset, int direct, int block, size_t smem, int* per_sm);
-cudaError_t launch_evaluate_parity(int opset, int direct, const EvalArgs& a, int block, int grid, size_t smem,
-                              cudaStream_t s);
 cudaError_t launch_predict_parity(int opset, const PredictArgs& a, int block, int grid, size_t smem, cudaStream_t s);
-cudaError_t launch_evaluate_batch_parity(int opset, int direct, const BatchArgs& a, int block, int grid,
-                                    size_t smem, cudaStream_t s);
-cudaError_t evaluate_occupancy_parity(int opset, int direct, int block, size_t smem, int* per_sm);
-cudaError_t evaluate_batch_occupancy_parity(int opset, int direct, int block, size_t smem, int* per_sm);
-cudaError_t launch_evaluate_native(int opset, int direct, const EvalArgs& a, int block, int grid, size_t smem,
-                              cudaStream_t s);
 cudaError_t launch_predict_native(int opset, const PredictArgs& a, int block, int grid, size_t smem, cudaStream_t s);
-cudaError_t launch_evaluate_batch_native(int opset, int direct, const BatchArgs& a, int block, int grid,
-                                    size_t smem, cudaStream_t s);
-cudaError_t evaluate_occupancy_native(int opset, int direct, int block, size_t smem, int* per_sm);
-cudaError_t evaluate_batch_occupancy_native(int opset, int direct, int block, size_t smem, int* per_sm);
 
 size_t evaluate_smem_bytes(int code_stride, int rows, int block, int R, int lanes, bool aligned) {
    const size_t T = (size_t)block * R;
@@ -40,10 +39,15 @@ size_t evaluate_smem_bytes(int code_stride, int rows, int block, int R, int lane
 
 cudaError_t launch_evaluate(int math, int opset, int direct, const EvalArgs& a, int block, int grid,
                             size_t smem, cudaStream_t s) {
+   const int k = direct & ~kOneLane;
+   const bool one = (direct & kOneLane) != 0;
    switch (math) {
-   case kMathParity: return launch_evaluate_parity(opset, direct, a, block, grid, smem, s);
-   case kMathNative: return launch_evaluate_native(opset, direct, a, block, grid, smem, s);
-   default: return launch_evaluate_fast(opset, direct, a, block, grid, smem, s);
+   case kMathParity: return one ? launch_evaluate_parity1(opset, k, a, block, grid, smem, s)
+                           : launch_evaluate_parity(opset, k, a, block, grid, smem, s);
+   case kMathNative: return one ? launch_evaluate_native1(opset, k, a, block, grid, smem, s)
+                           : launch_evaluate_native(opset, k, a, block, grid, smem, s);
+   default: return one ? launch_evaluate_fast1(opset, k, a, block, grid, smem, s)
+                           : launch_evaluate_fast(opset, k, a, block, grid, smem, s);
    }
 }
 
@@ -58,26 +62,41 @@ cudaError_t launch_predict(int math, int opset, const PredictArgs& a, int block,
 
 cudaError_t launch_evaluate_batch(int math, int opset, int direct, const BatchArgs& a, int block, int grid,
                                   size_t smem, cudaStream_t s) {
+   const int k = direct & ~kOneLane;
+   const bool one = (direct & kOneLane) != 0;
    switch (math) {
-   case kMathParity: return launch_evaluate_batch_parity(opset, direct, a, block, grid, smem, s);
-   case kMathNative: return launch_evaluate_batch_native(opset, direct, a, block, grid, smem, s);
-   default: return launch_evaluate_batch_fast(opset, direct, a, block, grid, smem, s);
+   case kMathParity: return one ? launch_evaluate_batch_parity1(opset, k, a, block, grid, smem, s)
+                           : launch_evaluate_batch_parity(opset, k, a, block, grid, smem, s);
+   case kMathNative: return one ? launch_evaluate_batch_native1(opset, k, a, block, grid, smem, s)
+                           : launch_evaluate_batch_native(opset, k, a, block, grid, smem, s);
+   default: return one ? launch_evaluate_batch_fast1(opset, k, a, block, grid, smem, s)
+                           : launch_evaluate_batch_fast(opset, k, a, block, grid, smem, s);
    }
 }
 
 cudaError_t evaluate_occupancy(int math, int opset, int direct, int block, size_t smem, int* per_sm) {
+   const int k = direct & ~kOneLane;
+   const bool one = (direct & kOneLane) != 0;
    switch (math) {
-   case kMathParity: return evaluate_occupancy_parity(opset, direct, block, smem, per_sm);
-   case kMathNative: return evaluate_occupancy_native(opset, direct, block, smem, per_sm);
-   default: return evaluate_occupancy_fast(opset, direct, block, smem, per_sm);
+   case kMathParity: return one ? evaluate_occupancy_parity1(opset, k, block, smem, per_sm)
+                           : evaluate_occupancy_parity(opset, k, block, smem, per_sm);
+   case kMathNative: return one ? evaluate_occupancy_native1(opset, k, block, smem, per_sm)
+                           : evaluate_occupancy_native(opset, k, block, smem, per_sm);
+   default: return one ? evaluate_occupancy_fast1(opset, k, block, smem, per_sm)
+                           : evaluate_occupancy_fast(opset, k, block, smem, per_sm);
    }
 }
 
 cudaError_t evaluate_batch_occupancy(int math, int opset, int direct, int block, size_t smem, int* per_sm) {
+   const int k = direct & ~kOneLane;
+   const bool one = (direct & kOneLane) != 0;
    switch (math) {
-   case kMathParity: return evaluate_batch_occupancy_parity(opset, direct, block, smem, per_sm);
-   case kMathNative: return evaluate_batch_occupancy_native(opset, direct, block, smem, per_sm);
-   default: return evaluate_batch_occupancy_fast(opset, direct, block, smem, per_sm);
+   case kMathParity: return one ? evaluate_batch_occupancy_parity1(opset, k, block, smem, per_sm)
+                           : evaluate_batch_occupancy_parity(opset, k, block, smem, per_sm);
+   case kMathNative: return one ? evaluate_batch_occupancy_native1(opset, k, block, smem, per_sm)
+                           : evaluate_batch_occupancy_native(opset, k, block, smem, per_sm);
+   default: return one ? evaluate_batch_occupancy_fast1(opset, k, block, smem, per_sm)
+                           : evaluate_batch_occupancy_fast(opset, k, block, smem, per_sm);
    }
 }
 
@@ -163,10 +182,12 @@ const char* plan_geometry(int strategy, int lanes, int math, int opset, int nlin
    const bool aligned = aligned_for(P);
    const int fit = std::min(rows_max, rows_fit(P));
    if (fit < 1) return "lane buffers do not fit in shared memory";
+   // one lane (PP, or PDP over one lane): the kernels with the one-lane chain
+   const int one = strategy != PPI_STRATEGY_DP && L == 1 ? kOneLane : 0;
    auto occupancy = [&](int direct, int rows) {
       int per_sm = 0;
       const size_t smem = evaluate_smem_bytes(code_stride, rows, P, R, L, aligned);
-      if (evaluate_occupancy(math, opset, direct, P, smem, &per_sm) != cudaSuccess) return 0;
+      if (evaluate_occupancy(math, opset, direct | one, P, smem, &per_sm) != cudaSuccess) return 0;
       return per_sm;
    };
    // the most rows at the occupancy of a one-row tile
@@ -219,13 +240,13 @@ const char* plan_geometry(int strategy, int lanes, int math, int opset, int nlin
    g->rows = rows;
    g->smem = evaluate_smem_bytes(code_stride, rows, P, R, L, aligned);
    g->per_sm[0] = occupancy(main_kernel, rows);
-   g->main_kernel = main_kernel;
+   g->main_kernel = main_kernel | one;
    if (g->per_sm[0] < 1) return "evaluator does not fit on an SM";
    g->grid = std::max(1, std::min(n_max, g->per_sm[0] * sm_count));
    g->wide = rows < rows_max;
    g->rows_wide = rows2;
    g->smem_wide = evaluate_smem_bytes(code_stride, rows2, P, R, L, aligned);
-   g->wide_kernel = wk;
+   g->wide_kernel = wk | one;
    g->per_sm[1] = occupancy(wk, rows2);
    if (g->per_sm[1] < 1) return "evaluator does not fit on an SM";
    g->grid_wide = std::max(1, std::min(n_max, g->per_sm[1] * sm_count));

@@ -527,7 +527,7 @@ struct Job {
 // target; row 0 is reused for the tile's errors once the program has run),
 // then, unless the lane == tile-position path applies, lanes floats of lane
 // accumulators and lanes bytes of lane-finished flags.
-template <int MATH, int R, int OPSET, int D>
+template <int MATH, int R, int OPSET, int D, int LANE1>
 __device__ float evaluate_program(const Job& j, uint2* s_code, float* s_tile, int* status, int tid,
                                   int P, Stager& st, float& sel, bool& abort) {
    const int T = P * R;
@@ -542,6 +542,10 @@ __device__ float evaluate_program(const Job& j, uint2* s_code, float* s_tile, in
    unsigned char* s_done = reinterpret_cast<unsigned char*>(s_acc + L);
    const int Teff = dp ? L * (T / L) : T;
    const float fnlin = (float)j.nlin;
+   // one lane (PP, or PDP over one lane) in a LANE1 kernel: the tile's first
+   // non-finite error, found by every thread
+   const bool one_lane = LANE1 && !dp && L == 1;
+   __shared__ int s_first;
    float fit = FLT_MAX;
    sel = FLT_MAX;
    if (kind == kKindInvalid || kind == kKindUnsupported) {
@@ -605,12 +609,16 @@ __device__ float evaluate_program(const Job& j, uint2* s_code, float* s_tile, in
          if (j.reduce_max) accumulate_lanes<1>(lacc, ldone, e, base, tid, P, T, j.nlin, fnlin);
          else accumulate_lanes<0>(lacc, ldone, e, base, tid, P, T, j.nlin, fnlin);
       } else {
+         if (one_lane && tid == 0) s_first = T;
          __syncthreads();   // every thread is done with the rows: row 0 takes the errors
+         int first = T;
 #pragma unroll
          for (int r = 0; r < R; ++r) {
             const int t = tile_pos(tid, r, P);
             s_err[t] = (dp && base + t >= j.nlin) ? 0.0f : e[r];
+            if (one_lane && base + t < j.nlin && nonfinite(e[r])) first = min(first, t);
          }
+         if (one_lane && first < T) atomicMin(&s_first, first);
          __syncthreads();
          if (dp) {
             const int G = Teff / L;
@@ -633,6 +641,34 @@ __device__ float evaluate_program(const Job& j, uint2* s_code, float* s_tile, in
                   if (nonfinite(part)) { dsum = FLT_MAX; ddone = true; }
                   else dsum = reduce1(j.reduce_max, dsum, part, fnlin);
                }
+            }
+         } else if (one_lane) {
+            // the one lane adds the tile's records in record order, up to the
+            // first non-finite error: a chain with no test in it, operands read
+            // four at a time (sequential.cc:171-179)
+            if (tid == 0 && !s_done[0]) {
+               const int cnt = min(T, j.nlin - base);
+               const int stop = min(cnt, s_first);
+               float acc = s_acc[0];
+               int n = 0;
+               if (j.reduce_max) {
+                  for (; n < stop; ++n) {
+                     const float v = s_err[n] * fnlin;
+                     acc = (v > acc) ? v : acc;
+                  }
+               } else {
+#pragma unroll 4
+                  for (; n + 4 <= stop; n += 4) {
+                     const float4 q = *reinterpret_cast<const float4*>(s_err + n);
+                     acc = acc + q.x;
+                     acc = acc + q.y;
+                     acc = acc + q.z;
+                     acc = acc + q.w;
+                  }
+                  for (; n < stop; ++n) acc = acc + s_err[n];
+               }
+               if (stop < cnt) { acc = FLT_MAX; s_done[0] = 1; }
+               s_acc[0] = acc;
             }
          } else {
             const int end = min(base + T, j.nlin);
@@ -688,7 +724,7 @@ __device__ float evaluate_program(const Job& j, uint2* s_code, float* s_tile, in
 // at a tile that still fits only 6 CTAs lost 4 % (the host picks).
 constexpr int min_ctas_per_sm(int math, int hi) { return math == kMathParity ? 4 : (hi ? 8 : 6); }
 
-template <int MATH, int R, int OPSET, int D, int HI>
+template <int MATH, int R, int OPSET, int D, int HI, int LANE1>
 __global__ void __launch_bounds__(128, min_ctas_per_sm(MATH, HI)) eval_kernel(const EvalArgs a) {
    extern __shared__ __align__(16) unsigned char smem_raw[];
    __shared__ int s_prog;
@@ -723,7 +759,7 @@ __global__ void __launch_bounds__(128, min_ctas_per_sm(MATH, HI)) eval_kernel(co
       j.code = a.code + (size_t)prog * a.code_stride;
       float sel;
       bool abort = false;
-      const float fit = evaluate_program<MATH, R, OPSET, D>(j, s_code, s_tile, a.status, tid, P, st, sel, abort);
+      const float fit = evaluate_program<MATH, R, OPSET, D, LANE1>(j, s_code, s_tile, a.status, tid, P, st, sel, abort);
       if (tid == 0) {
          a.fitness[prog] = fit;
          atomicMin(a.best_key, best_key(sel, best_tie(a.best, prog)));
@@ -745,7 +781,7 @@ __global__ void __launch_bounds__(128, min_ctas_per_sm(MATH, HI)) eval_kernel(co
 // in cost order (size x records, largest first); each population keeps its
 // own arg-min key and completion counter, and the CTA that finishes a
 // population's last program writes that population's best index.
-template <int MATH, int R, int OPSET, int D, int HI>
+template <int MATH, int R, int OPSET, int D, int HI, int LANE1>
 __global__ void __launch_bounds__(128, min_ctas_per_sm(MATH, HI)) eval_batch_kernel(const BatchArgs a) {
    extern __shared__ __align__(16) unsigned char smem_raw[];
    __shared__ int s_item;
@@ -779,7 +815,7 @@ __global__ void __launch_bounds__(128, min_ctas_per_sm(MATH, HI)) eval_batch_ker
       j.alpha_free = pd.best.alpha_free;
       float sel;
       bool abort = false;
-      const float fit = evaluate_program<MATH, R, OPSET, D>(j, s_code, s_tile, a.status, tid, P, st, sel, abort);
+      const float fit = evaluate_program<MATH, R, OPSET, D, LANE1>(j, s_code, s_tile, a.status, tid, P, st, sel, abort);
       if (abort) {   // staging failed: this CTA takes no more work
          if (tid == 0) a.fitness[g] = fit;
          break;
@@ -842,10 +878,13 @@ __global__ void __launch_bounds__(128, 4) predict_kernel(const PredictArgs a) {
 }
 
 
-// Per-math entry points, instantiated in evaluate_<math>.cu (R = kR records
-// per thread; opset 0 = FULL, 1 = ARITH; direct 0 = every column staged,
-// 1 = direct column reads compiled in).
-template <int MATH>
+// Per-math entry points, instantiated in evaluate_<math>.cu (LANE1 = 0) and
+// evaluate_<math>_lane1.cu (LANE1 = 1: the kernels with the one-lane chain,
+// for launches that hold a PP population; kept apart because the chain's
+// code changed the register allocation of every kernel that carried it, 3 %
+// on the uneven batch).  R = kR records per thread; opset 0 = FULL,
+// 1 = ARITH; the kernel id (`direct`) as kMainHi describes.
+template <int MATH, int LANE1>
 struct Launch {
    using EvalFn = void (*)(const EvalArgs);
    using BatchFn = void (*)(const BatchArgs);
@@ -857,19 +896,19 @@ struct Launch {
    template <int OPSET>
    static EvalFn eval_fn_set(int direct) {
       switch (direct) {
-      case 1: return eval_kernel<MATH, kR, OPSET, 1, 0>;
-      case 2: return eval_kernel<MATH, kR, OPSET, 2, 0>;
-      case kMainHi: return eval_kernel<MATH, kR, OPSET, 0, kHi>;
-      default: return eval_kernel<MATH, kR, OPSET, 0, 0>;
+      case 1: return eval_kernel<MATH, kR, OPSET, 1, 0, LANE1>;
+      case 2: return eval_kernel<MATH, kR, OPSET, 2, 0, LANE1>;
+      case kMainHi: return eval_kernel<MATH, kR, OPSET, 0, kHi, LANE1>;
+      default: return eval_kernel<MATH, kR, OPSET, 0, 0, LANE1>;
       }
    }
    template <int OPSET>
    static BatchFn batch_fn_set(int direct) {
       switch (direct) {
-      case 1: return eval_batch_kernel<MATH, kR, OPSET, 1, 0>;
-      case 2: return eval_batch_kernel<MATH, kR, OPSET, 2, 0>;
-      case kMainHi: return eval_batch_kernel<MATH, kR, OPSET, 0, kHi>;
-      default: return eval_batch_kernel<MATH, kR, OPSET, 0, 0>;
+      case 1: return eval_batch_kernel<MATH, kR, OPSET, 1, 0, LANE1>;
+      case 2: return eval_batch_kernel<MATH, kR, OPSET, 2, 0, LANE1>;
+      case kMainHi: return eval_batch_kernel<MATH, kR, OPSET, 0, kHi, LANE1>;
+      default: return eval_batch_kernel<MATH, kR, OPSET, 0, 0, LANE1>;
       }
    }
    static EvalFn eval_fn(int opset, int direct) {
@@ -929,3 +968,26 @@ struct Launch {
 
 }  // namespace ev
 }  // namespace ppi
+
+// Entry points of one math mode's kernel family (LANE1 = 0 or 1), with the
+// name suffix S: launch_evaluate_S, launch_evaluate_batch_S,
+// evaluate_occupancy_S, evaluate_batch_occupancy_S (evaluate.cu dispatches).
+#define PPI_EVALUATOR_ENTRY_POINTS(MATH, LANE1, S)                                             \
+   namespace ppi {                                                                            \
+   template struct ev::Launch<MATH, LANE1>;                                                   \
+   cudaError_t launch_evaluate_##S(int opset, int direct, const EvalArgs& a, int block, int grid, \
+                                   size_t smem, cudaStream_t s) {                             \
+      return ev::Launch<MATH, LANE1>::evaluate(opset, direct, a, block, grid, smem, s);       \
+   }                                                                                          \
+   cudaError_t launch_evaluate_batch_##S(int opset, int direct, const BatchArgs& a, int block,  \
+                                         int grid, size_t smem, cudaStream_t s) {             \
+      return ev::Launch<MATH, LANE1>::evaluate_batch(opset, direct, a, block, grid, smem, s); \
+   }                                                                                          \
+   cudaError_t evaluate_occupancy_##S(int opset, int direct, int block, size_t smem, int* per_sm) { \
+      return ev::Launch<MATH, LANE1>::occupancy(opset, direct, block, smem, per_sm);          \
+   }                                                                                          \
+   cudaError_t evaluate_batch_occupancy_##S(int opset, int direct, int block, size_t smem,      \
+                                            int* per_sm) {                                    \
+      return ev::Launch<MATH, LANE1>::occupancy_batch(opset, direct, block, smem, per_sm);    \
+   }                                                                                          \
+   }

@@ -30,8 +30,11 @@ constexpr int kColumnPad = 1024;
 enum : int { kOpsetFull = 0, kOpsetArith = 1 };
 // Evaluator kernel ids (the `direct` argument of the launchers): 0 the main
 // pass, 1 / 2 the wide pass (direct column reads: any tile / whole quads),
-// kMainHi the main pass built for 8 resident CTAs per SM (64 registers).
+// kMainHi the main pass built for 8 resident CTAs per SM (64 registers); with
+// kOneLane added, the same kernel with the one-lane chain (launches holding a
+// PP population, or PDP over one lane).
 constexpr int kMainHi = 3;
+constexpr int kOneLane = 4;
 
 // Program kinds written by the translator.  meta.x = kind | rows << 8, where
 // rows is the number of shared-memory rows the program's tile needs; meta.y is
@@ -524,6 +527,7 @@ struct Geometry {
    int per_sm[2] = {0, 0};     // resident CTAs per SM of the two passes
    int wide_kernel = 1;        // direct-read kernel of the wide pass: 2 whole quads (PP, PDP), 1 any tile
    int main_kernel = 0;        // kernel of the main pass: 0, or kMainHi when its tile fits more CTAs
+                               //   (both with kOneLane added for one lane)
 };
 // kOpsetArith when every op of the symbol table is in the ARITH set.
 int opset_for(const ppi_symbol_entry* symbols, int n);
