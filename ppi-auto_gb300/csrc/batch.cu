@@ -121,6 +121,7 @@ struct ppi_batch {
    float* h_fit = nullptr;
    int32_t* h_best = nullptr;
    int* h_status = nullptr;
+   ProgramUpload upload;   // host programs in compact form (upload.cu)
    cudaStream_t stream = nullptr;
    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
    // geometry
@@ -168,6 +169,7 @@ void bfree_all(ppi_batch* b) {
    cudaFree(b->d_ph); cudaFree(b->d_eph); cudaFree(b->d_size); cudaFree(b->d_fit);
    cudaFree(b->d_code); cudaFree(b->d_meta); cudaFree(b->d_work);
    cudaFreeHost(b->h_fit); cudaFreeHost(b->h_best); cudaFreeHost(b->h_status);
+   free_upload(&b->upload);
    if (b->ev0) cudaEventDestroy(b->ev0);
    if (b->ev1) cudaEventDestroy(b->ev1);
    if (b->stream) cudaStreamDestroy(b->stream);
@@ -547,10 +549,9 @@ ppi_status ppi_batch_evaluate(ppi_batch* b, const int32_t* ph, const float* eph,
                               float* fitness, int32_t* best_index, int32_t flags) {
    if (!b || !ph || !eph || !size || !fitness) return PPI_ERR_INVALID_ARGUMENT;
    PPI_BCUDA(b, cudaSetDevice(b->device));
-   const size_t T = (size_t)b->total, ms = (size_t)b->max_size;
-   PPI_BCUDA(b, cudaMemcpyAsync(b->d_ph, ph, T * ms * 4, cudaMemcpyHostToDevice, b->stream));
-   PPI_BCUDA(b, cudaMemcpyAsync(b->d_eph, eph, T * ms * 4, cudaMemcpyHostToDevice, b->stream));
-   PPI_BCUDA(b, cudaMemcpyAsync(b->d_size, size, T * 4, cudaMemcpyHostToDevice, b->stream));
+   const size_t T = (size_t)b->total;
+   PPI_BCUDA(b, upload_programs(&b->upload, ph, eph, size, b->total, b->max_size, b->d_ph, b->d_eph,
+                                b->d_size, b->sm_count, b->stream));
    ppi_status st = ppi_batch_evaluate_device(b, b->d_ph, b->d_eph, b->d_size, b->d_fit, b->d_best,
                                              b->stream, flags);
    if (st != PPI_OK) return st;

@@ -84,6 +84,7 @@ struct ppi_gpu {
    int* d_adj_order = nullptr;
    double* d_adj_psum = nullptr;   // per program and chunk: the constants' sums
    int* d_adj_pbad = nullptr;
+   ProgramUpload upload;   // host programs in compact form (upload.cu)
    size_t adj_chunk_cap = 0;       // program x chunk entries allocated
    std::vector<int2> h_adj_meta;
    std::vector<int> h_adj_order;
@@ -122,6 +123,7 @@ void free_all(ppi_gpu* h) {
    cudaFree(h->d_adj_code); cudaFree(h->d_adj_meta); cudaFree(h->d_grad); cudaFree(h->d_adj_stats);
    cudaFree(h->d_adj_order); cudaFree(h->d_adj_psum); cudaFree(h->d_adj_pbad);
    cudaFreeHost(h->h_adj_stats);
+   free_upload(&h->upload);
    if (h->ev0) cudaEventDestroy(h->ev0);
    if (h->ev1) cudaEventDestroy(h->ev1);
    if (h->evm) cudaEventDestroy(h->evm);
@@ -357,10 +359,8 @@ ppi_status ppi_gpu_evaluate_launch(ppi_gpu* h, const int32_t* ph, const float* e
    if (s != PPI_OK) return s;
    if (!ph || !eph || !size || !fitness) return fail(h, PPI_ERR_INVALID_ARGUMENT, "null argument");
    PPI_CUDA(h, cudaSetDevice(h->device));
-   const size_t ms = (size_t)h->cfg.max_size;
-   PPI_CUDA(h, cudaMemcpyAsync(h->d_ph, ph, (size_t)n * ms * 4, cudaMemcpyHostToDevice, h->stream));
-   PPI_CUDA(h, cudaMemcpyAsync(h->d_eph, eph, (size_t)n * ms * 4, cudaMemcpyHostToDevice, h->stream));
-   PPI_CUDA(h, cudaMemcpyAsync(h->d_size, size, (size_t)n * 4, cudaMemcpyHostToDevice, h->stream));
+   PPI_CUDA(h, upload_programs(&h->upload, ph, eph, size, n, h->cfg.max_size, h->d_ph, h->d_eph, h->d_size,
+                               h->sm_count, h->stream));
    s = enqueue(h, h->d_ph, h->d_eph, h->d_size, n, alpha, h->d_fit, h->d_best, h->stream);
    if (s != PPI_OK) return s;
    PPI_CUDA(h, cudaMemcpyAsync(h->h_fit, h->d_fit, (size_t)n * 4, cudaMemcpyDeviceToHost, h->stream));

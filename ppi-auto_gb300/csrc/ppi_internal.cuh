@@ -540,6 +540,21 @@ inline int max_program_rows(int ncol) { return kSlots + ncol + 1; }
 
 // Kernel launchers (evaluate.cu / translate.cu).
 cudaError_t launch_translate(int math, const TranslateArgs& a, cudaStream_t s);
+
+// Host programs to the device (upload.cu): the used prefix of each row packed
+// into a pinned staging area, one copy, then scattered into the device rows
+// (d_ph / d_eph rows of max_size; d_size gets the sizes).  The staging area
+// grows on demand and is reused: the caller must not start another upload on
+// it before the stream has passed this one.
+struct ProgramUpload {
+   void* h_stage = nullptr;   // pinned
+   void* d_stage = nullptr;
+   size_t cap = 0;
+};
+cudaError_t upload_programs(ProgramUpload* u, const int32_t* ph, const float* eph, const int32_t* size,
+                            int n, int max_size, int32_t* d_ph, float* d_eph, int32_t* d_size,
+                            int sm_count, cudaStream_t s);
+void free_upload(ProgramUpload* u);
 cudaError_t launch_evaluate(int math, int opset, int direct, const EvalArgs& a, int block, int grid,
                             size_t smem, cudaStream_t s);
 cudaError_t launch_predict(int math, int opset, const PredictArgs& a, int block, int grid, size_t smem,
