@@ -543,7 +543,8 @@ cudaError_t launch_translate(int math, const TranslateArgs& a, cudaStream_t s);
 
 // Host programs to the device (upload.cu): the used prefix of each row packed
 // into a pinned staging area, one copy, then scattered into the device rows
-// (d_ph / d_eph rows of max_size; d_size gets the sizes).  The staging area
+// (d_ph / d_eph rows of max_size; d_size gets the sizes); pinned rows of at
+// most 64 MB are copied as they are.  The staging area
 // grows on demand and is reused: the caller must not start another upload on
 // it before the stream has passed this one.
 struct ProgramUpload {

@@ -9,6 +9,7 @@
 // (threads over programs for large populations), copied in one transfer,
 // and scattered back into the device rows by a small kernel; the translator
 // reads tokens [0, size) of each row only, so the padding is never needed.
+// Rows already pinned and small in total go as they are.
 #include <algorithm>
 #include <cstring>
 #include <thread>
@@ -53,11 +54,27 @@ void free_upload(ProgramUpload* u) {
    u->cap = 0;
 }
 
+static bool pinned(const void* p) {
+   cudaPointerAttributes at{};
+   return cudaPointerGetAttributes(&at, p) == cudaSuccess && at.type == cudaMemoryTypeHost;
+}
+
 cudaError_t upload_programs(ProgramUpload* u, const int32_t* ph, const float* eph, const int32_t* size,
                             int n, int max_size, int32_t* d_ph, float* d_eph, int32_t* d_size,
                             int sm_count, cudaStream_t s) {
    if (n < 1) return cudaSuccess;
    const size_t ms = (size_t)max_size;
+   // Rows already in pinned memory, and few enough bytes that packing them on
+   // the host would cost more than sending the padding (measured: 30,000
+   // programs of at most 128 tokens, 1.2 ms of packing against 0.1 - 1 ms of
+   // padding), go as they are.
+   constexpr size_t kDirectBytes = 64u << 20;
+   if ((size_t)n * ms * 8 <= kDirectBytes && pinned(ph) && pinned(eph)) {
+      cudaError_t e = cudaMemcpyAsync(d_ph, ph, (size_t)n * ms * 4, cudaMemcpyHostToDevice, s);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(d_eph, eph, (size_t)n * ms * 4, cudaMemcpyHostToDevice, s);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(d_size, size, (size_t)n * 4, cudaMemcpyHostToDevice, s);
+      return e;
+   }
    // offsets of each program's used prefix (sizes outside [1, max_size] use none)
    std::vector<long long> off((size_t)n);
    long long total = 0;
