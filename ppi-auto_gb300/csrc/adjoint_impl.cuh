@@ -271,8 +271,14 @@ __device__ __forceinline__ void adj_reverse(const uint2* __restrict__ code, floa
    }
 }
 
+// Register bound: 4 records per thread fit 64 registers (8 CTAs per SM where
+// the tile allows, no spills in fast math), measured 1.6 % faster on the
+// 100k x 8 adjoint workload than the 4-CTA bound; 8 records keep 4 CTAs.
+template <int R>
+constexpr int adjoint_min_ctas() { return R == 4 ? 8 : 4; }
+
 template <int MATH, int OPSET, int R>
-__global__ void __launch_bounds__(128, 4) adjoint_kernel(const AdjointArgs a) {
+__global__ void __launch_bounds__(128, adjoint_min_ctas<R>()) adjoint_kernel(const AdjointArgs a) {
    extern __shared__ __align__(16) unsigned char smem_raw[];
    __shared__ int s_prog, s_bad;
    __shared__ __align__(8) uint64_t s_bar;

@@ -461,7 +461,7 @@ constexpr int kAdjLevels = 16;
 // at most), so the constant-adjoint workload (100k x 8, 10000 programs) runs
 // at R = 4, measured 2.6 % faster than with R = 8 kept from 4 CTAs up.
 constexpr int kAdjR8MinCtas = 6;
-constexpr int kAdjMaxChunks = 16;   // record chunks (work items) per program
+constexpr int kAdjMaxChunks = 32;   // record chunks (work items) per program
 constexpr int kAdjStats = 3 + 2 * kAdjLevels;
 
 ppi_status ppi_gpu_constant_gradient(ppi_gpu* h, const int32_t* ph, const float* eph,
@@ -553,7 +553,7 @@ ppi_status ppi_gpu_constant_gradient(ppi_gpu* h, const int32_t* ph, const float*
                        [&](int x, int y) { return size[x] > size[y]; });
    // chunks of each program's records (work items): about 8 tiles or more
    // each, at most kAdjMaxChunks per program
-   const int n_chunks = std::max(1, std::min(kAdjMaxChunks, (h->nlin + 8191) / 8192));
+   const int n_chunks = std::max(1, std::min(kAdjMaxChunks, (h->nlin + 4095) / 4096));
    const int chunk = ((h->nlin + n_chunks - 1) / n_chunks + 1023) / 1024 * 1024;
    const int chunks = (h->nlin + chunk - 1) / chunk;
    const size_t entries = (size_t)n * chunks;
