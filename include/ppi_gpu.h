@@ -237,6 +237,13 @@ int32_t ppi_gpu_lanes(const ppi_gpu* h);
 /* Number of kernel launches the last evaluate / predict / decode call made. */
 int32_t ppi_gpu_last_launch_count(const ppi_gpu* h);
 
+/* Launch plan for the current dataset (no reference counterpart: the
+ * evaluator's own geometry).  Each output may be NULL: block the threads per
+ * CTA, rows the main pass's tile rows, n_chunks the record chunks a program is
+ * evaluated in (1, or more when the programs walk a dataset larger than L2
+ * together, chunk by chunk).  PPI_ERR_NOT_READY before a dataset is set. */
+ppi_status ppi_gpu_geometry(const ppi_gpu* h, int32_t* block, int32_t* rows, int32_t* n_chunks);
+
 /* Inspection of the last evaluate call's translation (waits for it).  No
  * reference counterpart: the bytecode is this library's own.  code_stride
  * receives the uint2 words of one program's code; opset the opcode set of the

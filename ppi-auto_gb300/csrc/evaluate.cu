@@ -9,8 +9,8 @@
 
 namespace ppi {
 
-// Entry points of evaluate_<math>.cu (suffix <math>) and evaluate_<math>_lane1.cu
-// (suffix <math>1).
+// Entry points of evaluate_<math>.cu (suffix <math>), evaluate_<math>_lane1.cu
+// (suffix <math>1) and evaluate_<math>_chunk.cu (suffix <math>2).
 #define PPI_DECLARE_ENTRY_POINTS(S)                                                             \
    cudaError_t launch_evaluate_##S(int opset, int direct, const EvalArgs& a, int block, int grid, \
                                    size_t smem, cudaStream_t s);                              \
@@ -20,10 +20,13 @@ namespace ppi {
    cudaError_t evaluate_batch_occupancy_##S(int opset, int direct, int block, size_t smem, int* per_sm);
 PPI_DECLARE_ENTRY_POINTS(fast)
 PPI_DECLARE_ENTRY_POINTS(fast1)
+PPI_DECLARE_ENTRY_POINTS(fast2)
 PPI_DECLARE_ENTRY_POINTS(parity)
 PPI_DECLARE_ENTRY_POINTS(parity1)
+PPI_DECLARE_ENTRY_POINTS(parity2)
 PPI_DECLARE_ENTRY_POINTS(native)
 PPI_DECLARE_ENTRY_POINTS(native1)
+PPI_DECLARE_ENTRY_POINTS(native2)
 #undef PPI_DECLARE_ENTRY_POINTS
 cudaError_t launch_predict_fast(int opset, const PredictArgs& a, int block, int grid, size_t smem, cudaStream_t s);
 cudaError_t launch_predict_parity(int opset, const PredictArgs& a, int block, int grid, size_t smem, cudaStream_t s);
@@ -39,14 +42,17 @@ size_t evaluate_smem_bytes(int code_stride, int rows, int block, int R, int lane
 
 cudaError_t launch_evaluate(int math, int opset, int direct, const EvalArgs& a, int block, int grid,
                             size_t smem, cudaStream_t s) {
-   const int k = direct & ~kOneLane;
-   const bool one = (direct & kOneLane) != 0;
+   const int k = direct & ~(kOneLane | kChunked);
+   const int fam = (direct & kOneLane) ? 1 : ((direct & kChunked) ? 2 : 0);
    switch (math) {
-   case kMathParity: return one ? launch_evaluate_parity1(opset, k, a, block, grid, smem, s)
+   case kMathParity: return fam == 1 ? launch_evaluate_parity1(opset, k, a, block, grid, smem, s)
+                           : fam == 2 ? launch_evaluate_parity2(opset, k, a, block, grid, smem, s)
                            : launch_evaluate_parity(opset, k, a, block, grid, smem, s);
-   case kMathNative: return one ? launch_evaluate_native1(opset, k, a, block, grid, smem, s)
+   case kMathNative: return fam == 1 ? launch_evaluate_native1(opset, k, a, block, grid, smem, s)
+                           : fam == 2 ? launch_evaluate_native2(opset, k, a, block, grid, smem, s)
                            : launch_evaluate_native(opset, k, a, block, grid, smem, s);
-   default: return one ? launch_evaluate_fast1(opset, k, a, block, grid, smem, s)
+   default: return fam == 1 ? launch_evaluate_fast1(opset, k, a, block, grid, smem, s)
+                           : fam == 2 ? launch_evaluate_fast2(opset, k, a, block, grid, smem, s)
                            : launch_evaluate_fast(opset, k, a, block, grid, smem, s);
    }
 }
@@ -62,40 +68,49 @@ cudaError_t launch_predict(int math, int opset, const PredictArgs& a, int block,
 
 cudaError_t launch_evaluate_batch(int math, int opset, int direct, const BatchArgs& a, int block, int grid,
                                   size_t smem, cudaStream_t s) {
-   const int k = direct & ~kOneLane;
-   const bool one = (direct & kOneLane) != 0;
+   const int k = direct & ~(kOneLane | kChunked);
+   const int fam = (direct & kOneLane) ? 1 : ((direct & kChunked) ? 2 : 0);
    switch (math) {
-   case kMathParity: return one ? launch_evaluate_batch_parity1(opset, k, a, block, grid, smem, s)
+   case kMathParity: return fam == 1 ? launch_evaluate_batch_parity1(opset, k, a, block, grid, smem, s)
+                           : fam == 2 ? launch_evaluate_batch_parity2(opset, k, a, block, grid, smem, s)
                            : launch_evaluate_batch_parity(opset, k, a, block, grid, smem, s);
-   case kMathNative: return one ? launch_evaluate_batch_native1(opset, k, a, block, grid, smem, s)
+   case kMathNative: return fam == 1 ? launch_evaluate_batch_native1(opset, k, a, block, grid, smem, s)
+                           : fam == 2 ? launch_evaluate_batch_native2(opset, k, a, block, grid, smem, s)
                            : launch_evaluate_batch_native(opset, k, a, block, grid, smem, s);
-   default: return one ? launch_evaluate_batch_fast1(opset, k, a, block, grid, smem, s)
+   default: return fam == 1 ? launch_evaluate_batch_fast1(opset, k, a, block, grid, smem, s)
+                           : fam == 2 ? launch_evaluate_batch_fast2(opset, k, a, block, grid, smem, s)
                            : launch_evaluate_batch_fast(opset, k, a, block, grid, smem, s);
    }
 }
 
 cudaError_t evaluate_occupancy(int math, int opset, int direct, int block, size_t smem, int* per_sm) {
-   const int k = direct & ~kOneLane;
-   const bool one = (direct & kOneLane) != 0;
+   const int k = direct & ~(kOneLane | kChunked);
+   const int fam = (direct & kOneLane) ? 1 : ((direct & kChunked) ? 2 : 0);
    switch (math) {
-   case kMathParity: return one ? evaluate_occupancy_parity1(opset, k, block, smem, per_sm)
+   case kMathParity: return fam == 1 ? evaluate_occupancy_parity1(opset, k, block, smem, per_sm)
+                           : fam == 2 ? evaluate_occupancy_parity2(opset, k, block, smem, per_sm)
                            : evaluate_occupancy_parity(opset, k, block, smem, per_sm);
-   case kMathNative: return one ? evaluate_occupancy_native1(opset, k, block, smem, per_sm)
+   case kMathNative: return fam == 1 ? evaluate_occupancy_native1(opset, k, block, smem, per_sm)
+                           : fam == 2 ? evaluate_occupancy_native2(opset, k, block, smem, per_sm)
                            : evaluate_occupancy_native(opset, k, block, smem, per_sm);
-   default: return one ? evaluate_occupancy_fast1(opset, k, block, smem, per_sm)
+   default: return fam == 1 ? evaluate_occupancy_fast1(opset, k, block, smem, per_sm)
+                           : fam == 2 ? evaluate_occupancy_fast2(opset, k, block, smem, per_sm)
                            : evaluate_occupancy_fast(opset, k, block, smem, per_sm);
    }
 }
 
 cudaError_t evaluate_batch_occupancy(int math, int opset, int direct, int block, size_t smem, int* per_sm) {
-   const int k = direct & ~kOneLane;
-   const bool one = (direct & kOneLane) != 0;
+   const int k = direct & ~(kOneLane | kChunked);
+   const int fam = (direct & kOneLane) ? 1 : ((direct & kChunked) ? 2 : 0);
    switch (math) {
-   case kMathParity: return one ? evaluate_batch_occupancy_parity1(opset, k, block, smem, per_sm)
+   case kMathParity: return fam == 1 ? evaluate_batch_occupancy_parity1(opset, k, block, smem, per_sm)
+                           : fam == 2 ? evaluate_batch_occupancy_parity2(opset, k, block, smem, per_sm)
                            : evaluate_batch_occupancy_parity(opset, k, block, smem, per_sm);
-   case kMathNative: return one ? evaluate_batch_occupancy_native1(opset, k, block, smem, per_sm)
+   case kMathNative: return fam == 1 ? evaluate_batch_occupancy_native1(opset, k, block, smem, per_sm)
+                           : fam == 2 ? evaluate_batch_occupancy_native2(opset, k, block, smem, per_sm)
                            : evaluate_batch_occupancy_native(opset, k, block, smem, per_sm);
-   default: return one ? evaluate_batch_occupancy_fast1(opset, k, block, smem, per_sm)
+   default: return fam == 1 ? evaluate_batch_occupancy_fast1(opset, k, block, smem, per_sm)
+                           : fam == 2 ? evaluate_batch_occupancy_fast2(opset, k, block, smem, per_sm)
                            : evaluate_batch_occupancy_fast(opset, k, block, smem, per_sm);
    }
 }
@@ -151,7 +166,7 @@ const char* best_geometry(int rule, int group, int strategy, int n, BestGeo* out
 }
 
 const char* plan_geometry(int strategy, int lanes, int math, int opset, int nlin, int ncol,
-                          int code_stride, int n_max, int sm_count, Geometry* g) {
+                          int code_stride, int n_max, int sm_count, Geometry* g, bool allow_chunk) {
    const int L = lanes;
    if (L < 1 || L > kMaxLanes) return "lane count out of range";
    // records per thread: kR (8 measured faster than 16 on GB300: more
@@ -182,8 +197,13 @@ const char* plan_geometry(int strategy, int lanes, int math, int opset, int nlin
    const bool aligned = aligned_for(P);
    const int fit = std::min(rows_max, rows_fit(P));
    if (fit < 1) return "lane buffers do not fit in shared memory";
-   // one lane (PP, or PDP over one lane): the kernels with the one-lane chain
-   const int one = strategy != PPI_STRATEGY_DP && L == 1 ? kOneLane : 0;
+   // one lane (PP, or PDP over one lane): the kernels with the one-lane chain;
+   // lane == tile position over a dataset larger than L2: the chunked kernels
+   // (every program walks the same records at about the same time, so a
+   // record chunk comes from DRAM once and from L2 for the other programs)
+   const bool chunk = allow_chunk && strategy == PPI_STRATEGY_PDP && aligned_for(P) &&
+                      (size_t)nlin * ncol * 4 >= kChunkMinBytes;
+   const int one = strategy != PPI_STRATEGY_DP && L == 1 ? kOneLane : (chunk ? kChunked : 0);
    auto occupancy = [&](int direct, int rows) {
       int per_sm = 0;
       const size_t smem = evaluate_smem_bytes(code_stride, rows, P, R, L, aligned);
@@ -247,6 +267,9 @@ const char* plan_geometry(int strategy, int lanes, int math, int opset, int nlin
    g->rows_wide = rows2;
    g->smem_wide = evaluate_smem_bytes(code_stride, rows2, P, R, L, aligned);
    g->wide_kernel = wk | one;
+   g->chunked = chunk;
+   g->chunk_records = kChunkTiles * P * R;
+   g->n_chunks = chunk ? (nlin + g->chunk_records - 1) / g->chunk_records : 1;
    g->per_sm[1] = occupancy(wk, rows2);
    if (g->per_sm[1] < 1) return "evaluator does not fit on an SM";
    g->grid_wide = std::max(1, std::min(n_max, g->per_sm[1] * sm_count));

@@ -515,6 +515,8 @@ struct Job {
    int rows_cap;               // tile rows of this pass (lane accumulators follow them)
    int code_cap;               // words of the shared-memory code region
    int alpha_free;             // the best index compares error/nlin without alpha*size
+   int r0, r1;                 // chunked kernels: this item's records [r0, r1)
+   float* state;               // chunked kernels: the program's lane state, (R + 1) x P floats
 };
 
 // Fitness of one program (valid in thread 0), in exactly the reference
@@ -527,7 +529,7 @@ struct Job {
 // target; row 0 is reused for the tile's errors once the program has run),
 // then, unless the lane == tile-position path applies, lanes floats of lane
 // accumulators and lanes bytes of lane-finished flags.
-template <int MATH, int R, int OPSET, int D, int LANE1>
+template <int MATH, int R, int OPSET, int D, int FAMILY>
 __device__ float evaluate_program(const Job& j, uint2* s_code, float* s_tile, int* status, int tid,
                                   int P, Stager& st, float& sel, bool& abort) {
    const int T = P * R;
@@ -542,9 +544,14 @@ __device__ float evaluate_program(const Job& j, uint2* s_code, float* s_tile, in
    unsigned char* s_done = reinterpret_cast<unsigned char*>(s_acc + L);
    const int Teff = dp ? L * (T / L) : T;
    const float fnlin = (float)j.nlin;
-   // one lane (PP, or PDP over one lane) in a LANE1 kernel: the tile's first
-   // non-finite error, found by every thread
-   const bool one_lane = LANE1 && !dp && L == 1;
+   // one lane (PP, or PDP over one lane) in a one-lane kernel: the tile's
+   // first non-finite error, found by every thread
+   const bool one_lane = FAMILY == kFamilyOneLane && !dp && L == 1;
+   // a chunked kernel evaluates records [r0, r1) (lane == tile position),
+   // the lane state coming from and going to j.state between chunks
+   constexpr bool chunked = FAMILY == kFamilyChunked;
+   const int r0 = chunked ? j.r0 : 0;
+   const int r1 = chunked ? j.r1 : j.nlin;
    __shared__ int s_first;
    float fit = FLT_MAX;
    sel = FLT_MAX;
@@ -575,9 +582,16 @@ __device__ float evaluate_program(const Job& j, uint2* s_code, float* s_tile, in
 #pragma unroll
    for (int r = 0; r < R; ++r) lacc[r] = 0.0f;
    uint32_t ldone = 0u;
+   if constexpr (chunked) {
+      if (r0 > 0) {   // the lanes as the previous chunk left them (bypassing L1)
+#pragma unroll
+         for (int r = 0; r < R; ++r) lacc[r] = __ldcg(j.state + (size_t)r * P + tid);
+         ldone = __float_as_uint(__ldcg(j.state + (size_t)R * P + tid));
+      }
+   }
    float dsum = 0.0f;
    bool ddone = false;
-   for (int base = 0; base < j.nlin; base += Teff) {
+   for (int base = r0; base < r1; base += Teff) {
       __syncthreads();
       if (!stage_tile(j.data, j.ncol, j.ld, s_code, s_tile, base, T, tid, P, st, status)) {
          // the tile never arrived (status recorded): no fitness for this
@@ -688,6 +702,15 @@ __device__ float evaluate_program(const Job& j, uint2* s_code, float* s_tile, in
          }
       }
    }
+   if constexpr (chunked) {
+      if (r1 < j.nlin) {   // not the last chunk: keep the lanes for the next one
+#pragma unroll
+         for (int r = 0; r < R; ++r) __stcg(j.state + (size_t)r * P + tid, lacc[r]);
+         __stcg(j.state + (size_t)R * P + tid, __uint_as_float(ldone));
+         __syncthreads();
+         return fit;
+      }
+   }
    __syncthreads();
    if (dp) {
       if (tid == 0) {
@@ -713,6 +736,10 @@ __device__ float evaluate_program(const Job& j, uint2* s_code, float* s_tile, in
    return fit;
 }
 
+// Waits of a chunked item for its program's previous chunk (each with a
+// 256 ns sleep): about a second, then kStatusChunkWait and the CTA stops.
+constexpr int kChunkWaitLimit = 1 << 22;
+
 // One population: a persistent grid pulls program indices from a device
 // counter; the last CTA to finish turns the packed arg-min into the index.
 // Resident CTAs per SM the register allocation is bounded for: the fast and
@@ -724,7 +751,7 @@ __device__ float evaluate_program(const Job& j, uint2* s_code, float* s_tile, in
 // at a tile that still fits only 6 CTAs lost 4 % (the host picks).
 constexpr int min_ctas_per_sm(int math, int hi) { return math == kMathParity ? 4 : (hi ? 8 : 6); }
 
-template <int MATH, int R, int OPSET, int D, int HI, int LANE1>
+template <int MATH, int R, int OPSET, int D, int HI, int FAMILY>
 __global__ void __launch_bounds__(128, min_ctas_per_sm(MATH, HI)) eval_kernel(const EvalArgs a) {
    extern __shared__ __align__(16) unsigned char smem_raw[];
    __shared__ int s_prog;
@@ -744,22 +771,62 @@ __global__ void __launch_bounds__(128, min_ctas_per_sm(MATH, HI)) eval_kernel(co
    j.alpha_free = a.best.alpha_free;
    unsigned* queue = a.wide_pass ? &a.stats->wide_queue : &a.stats->queue;
    const int limit = a.wide_pass ? (int)a.stats->wide : a.n;
+   // chunked kernels: work items (program, record chunk) in chunk-major order,
+   // so that the grid walks the dataset together; a chunk waits (bounded) for
+   // its program's previous chunk, which an earlier item holds
+   constexpr bool chunked = FAMILY == kFamilyChunked;
+   const long long items = chunked ? (long long)limit * a.n_chunks : limit;
+   __shared__ int s_wait_failed;
    for (;;) {
       if (tid == 0) s_prog = (int)atomicAdd(queue, 1u);
       __syncthreads();
       const int item = s_prog;
-      if (item >= limit) break;
-      const int prog = a.wide_pass ? a.wide_list[item] : item;
+      if (item >= items) break;
+      const int c = chunked ? item / limit : 0;
+      const int k = chunked ? item - c * limit : item;
+      const int prog = a.wide_pass ? a.wide_list[k] : k;
       j.meta = a.meta[prog];
-      if (!a.wide_pass && meta_kind(j.meta) == kKindWide) {
+      const int kind = meta_kind(j.meta);
+      if ((!a.wide_pass && kind == kKindWide) ||
+          (chunked && c > 0 && (kind == kKindInvalid || kind == kKindUnsupported))) {
          __syncthreads();   // s_prog is read by every thread before it is rewritten
          continue;
       }
       j.size = a.size[prog];
       j.code = a.code + (size_t)prog * a.code_stride;
+      bool last = true;
+      if constexpr (chunked) {
+         j.r0 = c * a.chunk_records;
+         j.r1 = min(a.nlin, j.r0 + a.chunk_records);
+         j.state = a.chunk_state + (size_t)prog * (R + 1) * P;
+         last = j.r1 >= a.nlin || kind == kKindInvalid || kind == kKindUnsupported;
+         if (c > 0) {
+            if (tid == 0) {
+               volatile unsigned* done = a.chunk_done + prog;
+               int it = 0;
+               while (*done < (unsigned)c && it < kChunkWaitLimit) {
+                  __nanosleep(256);
+                  ++it;
+               }
+               s_wait_failed = *done < (unsigned)c;
+               if (s_wait_failed) atomicOr(a.status, kStatusChunkWait);
+               __threadfence();
+            }
+            __syncthreads();
+            if (s_wait_failed) break;   // this CTA takes no more work
+         }
+      }
       float sel;
       bool abort = false;
-      const float fit = evaluate_program<MATH, R, OPSET, D, LANE1>(j, s_code, s_tile, a.status, tid, P, st, sel, abort);
+      const float fit = evaluate_program<MATH, R, OPSET, D, FAMILY>(j, s_code, s_tile, a.status, tid, P, st, sel, abort);
+      if (!last) {
+         if (abort) break;   // no state stored: the next chunk times out (status recorded)
+         // the lane state is stored: publish this chunk to the program's next one
+         __threadfence();
+         __syncthreads();
+         if (tid == 0) atomicExch(a.chunk_done + prog, (unsigned)(c + 1));
+         continue;
+      }
       if (tid == 0) {
          a.fitness[prog] = fit;
          atomicMin(a.best_key, best_key(sel, best_tie(a.best, prog)));
@@ -781,7 +848,7 @@ __global__ void __launch_bounds__(128, min_ctas_per_sm(MATH, HI)) eval_kernel(co
 // in cost order (size x records, largest first); each population keeps its
 // own arg-min key and completion counter, and the CTA that finishes a
 // population's last program writes that population's best index.
-template <int MATH, int R, int OPSET, int D, int HI, int LANE1>
+template <int MATH, int R, int OPSET, int D, int HI, int FAMILY>
 __global__ void __launch_bounds__(128, min_ctas_per_sm(MATH, HI)) eval_batch_kernel(const BatchArgs a) {
    extern __shared__ __align__(16) unsigned char smem_raw[];
    __shared__ int s_item;
@@ -815,7 +882,7 @@ __global__ void __launch_bounds__(128, min_ctas_per_sm(MATH, HI)) eval_batch_ker
       j.alpha_free = pd.best.alpha_free;
       float sel;
       bool abort = false;
-      const float fit = evaluate_program<MATH, R, OPSET, D, LANE1>(j, s_code, s_tile, a.status, tid, P, st, sel, abort);
+      const float fit = evaluate_program<MATH, R, OPSET, D, FAMILY>(j, s_code, s_tile, a.status, tid, P, st, sel, abort);
       if (abort) {   // staging failed: this CTA takes no more work
          if (tid == 0) a.fitness[g] = fit;
          break;
@@ -878,13 +945,14 @@ __global__ void __launch_bounds__(128, 4) predict_kernel(const PredictArgs a) {
 }
 
 
-// Per-math entry points, instantiated in evaluate_<math>.cu (LANE1 = 0) and
-// evaluate_<math>_lane1.cu (LANE1 = 1: the kernels with the one-lane chain,
+// Per-math entry points, instantiated in evaluate_<math>.cu (FAMILY = 0),
+// evaluate_<math>_chunk.cu (FAMILY = 2: the chunked kernels) and
+// evaluate_<math>_lane1.cu (FAMILY = 1: the kernels with the one-lane chain,
 // for launches that hold a PP population; kept apart because the chain's
 // code changed the register allocation of every kernel that carried it, 3 %
 // on the uneven batch).  R = kR records per thread; opset 0 = FULL,
 // 1 = ARITH; the kernel id (`direct`) as kMainHi describes.
-template <int MATH, int LANE1>
+template <int MATH, int FAMILY>
 struct Launch {
    using EvalFn = void (*)(const EvalArgs);
    using BatchFn = void (*)(const BatchArgs);
@@ -896,19 +964,21 @@ struct Launch {
    template <int OPSET>
    static EvalFn eval_fn_set(int direct) {
       switch (direct) {
-      case 1: return eval_kernel<MATH, kR, OPSET, 1, 0, LANE1>;
-      case 2: return eval_kernel<MATH, kR, OPSET, 2, 0, LANE1>;
-      case kMainHi: return eval_kernel<MATH, kR, OPSET, 0, kHi, LANE1>;
-      default: return eval_kernel<MATH, kR, OPSET, 0, 0, LANE1>;
+      case 1: return eval_kernel<MATH, kR, OPSET, 1, 0, FAMILY>;
+      case 2: return eval_kernel<MATH, kR, OPSET, 2, 0, FAMILY>;
+      case kMainHi: return eval_kernel<MATH, kR, OPSET, 0, kHi, FAMILY>;
+      default: return eval_kernel<MATH, kR, OPSET, 0, 0, FAMILY>;
       }
    }
+   // (batches have no chunked kernels: that family's entries are the plain ones)
+   static constexpr int kBatchFamily = FAMILY == kFamilyChunked ? kFamilyPlain : FAMILY;
    template <int OPSET>
    static BatchFn batch_fn_set(int direct) {
       switch (direct) {
-      case 1: return eval_batch_kernel<MATH, kR, OPSET, 1, 0, LANE1>;
-      case 2: return eval_batch_kernel<MATH, kR, OPSET, 2, 0, LANE1>;
-      case kMainHi: return eval_batch_kernel<MATH, kR, OPSET, 0, kHi, LANE1>;
-      default: return eval_batch_kernel<MATH, kR, OPSET, 0, 0, LANE1>;
+      case 1: return eval_batch_kernel<MATH, kR, OPSET, 1, 0, kBatchFamily>;
+      case 2: return eval_batch_kernel<MATH, kR, OPSET, 2, 0, kBatchFamily>;
+      case kMainHi: return eval_batch_kernel<MATH, kR, OPSET, 0, kHi, kBatchFamily>;
+      default: return eval_batch_kernel<MATH, kR, OPSET, 0, 0, kBatchFamily>;
       }
    }
    static EvalFn eval_fn(int opset, int direct) {
@@ -969,25 +1039,25 @@ struct Launch {
 }  // namespace ev
 }  // namespace ppi
 
-// Entry points of one math mode's kernel family (LANE1 = 0 or 1), with the
+// Entry points of one math mode's kernel family (kFamily*), with the
 // name suffix S: launch_evaluate_S, launch_evaluate_batch_S,
 // evaluate_occupancy_S, evaluate_batch_occupancy_S (evaluate.cu dispatches).
-#define PPI_EVALUATOR_ENTRY_POINTS(MATH, LANE1, S)                                             \
+#define PPI_EVALUATOR_ENTRY_POINTS(MATH, FAMILY, S)                                             \
    namespace ppi {                                                                            \
-   template struct ev::Launch<MATH, LANE1>;                                                   \
+   template struct ev::Launch<MATH, FAMILY>;                                                   \
    cudaError_t launch_evaluate_##S(int opset, int direct, const EvalArgs& a, int block, int grid, \
                                    size_t smem, cudaStream_t s) {                             \
-      return ev::Launch<MATH, LANE1>::evaluate(opset, direct, a, block, grid, smem, s);       \
+      return ev::Launch<MATH, FAMILY>::evaluate(opset, direct, a, block, grid, smem, s);       \
    }                                                                                          \
    cudaError_t launch_evaluate_batch_##S(int opset, int direct, const BatchArgs& a, int block,  \
                                          int grid, size_t smem, cudaStream_t s) {             \
-      return ev::Launch<MATH, LANE1>::evaluate_batch(opset, direct, a, block, grid, smem, s); \
+      return ev::Launch<MATH, FAMILY>::evaluate_batch(opset, direct, a, block, grid, smem, s); \
    }                                                                                          \
    cudaError_t evaluate_occupancy_##S(int opset, int direct, int block, size_t smem, int* per_sm) { \
-      return ev::Launch<MATH, LANE1>::occupancy(opset, direct, block, smem, per_sm);          \
+      return ev::Launch<MATH, FAMILY>::occupancy(opset, direct, block, smem, per_sm);          \
    }                                                                                          \
    cudaError_t evaluate_batch_occupancy_##S(int opset, int direct, int block, size_t smem,      \
                                             int* per_sm) {                                    \
-      return ev::Launch<MATH, LANE1>::occupancy_batch(opset, direct, block, smem, per_sm);    \
+      return ev::Launch<MATH, FAMILY>::occupancy_batch(opset, direct, block, smem, per_sm);    \
    }                                                                                          \
    }

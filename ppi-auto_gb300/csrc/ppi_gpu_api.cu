@@ -54,6 +54,11 @@ struct ppi_gpu {
    unsigned long long* d_key = nullptr;
    DevStats* d_stats = nullptr;
    int* d_wide = nullptr;
+   // chunked evaluation (Geometry::chunked): lane state and finished-chunk
+   // counters, one per program
+   float* d_chunk_state = nullptr;
+   unsigned* d_chunk_done = nullptr;
+   size_t chunk_cap = 0;
    int32_t* d_best = nullptr;
    int* d_status = nullptr;
    float* d_pred = nullptr;
@@ -117,6 +122,7 @@ void free_all(ppi_gpu* h) {
    cudaFree(h->d_ph); cudaFree(h->d_eph); cudaFree(h->d_size); cudaFree(h->d_code);
    cudaFree(h->d_meta); cudaFree(h->d_work); cudaFree(h->d_fit); cudaFree(h->d_key);
    cudaFree(h->d_stats); cudaFree(h->d_wide); cudaFree(h->d_best); cudaFree(h->d_status); cudaFree(h->d_pred);
+   cudaFree(h->d_chunk_state); cudaFree(h->d_chunk_done);
    cudaFree(h->d_genomes); cudaFree(h->d_frames);
    free_decode_tables(&h->dec);
    cudaFreeHost(h->h_fit); cudaFreeHost(h->h_best); cudaFreeHost(h->h_status);
@@ -134,8 +140,24 @@ void free_all(ppi_gpu* h) {
 ppi_status plan(ppi_gpu* h) {
    Geometry g;
    const char* why = plan_geometry(h->cfg.strategy, h->lanes, h->cfg.math, h->opset, h->nlin,
-                                   h->ncol, h->code_stride, h->cfg.population_size, h->sm_count, &g);
+                                   h->ncol, h->code_stride, h->cfg.population_size, h->sm_count, &g,
+                                   true);
    if (why) return fail(h, PPI_ERR_UNSUPPORTED, why);
+   if (g.chunked) {
+      // each program's lane state between chunks: R + 1 floats per thread
+      const size_t per = (size_t)(g.R + 1) * g.block, pop = (size_t)h->cfg.population_size;
+      if (pop * per > h->chunk_cap) {
+         PPI_CUDA(h, cudaSetDevice(h->device));
+         cudaFree(h->d_chunk_state);
+         cudaFree(h->d_chunk_done);
+         h->d_chunk_state = nullptr;
+         h->d_chunk_done = nullptr;
+         h->chunk_cap = 0;
+         PPI_CUDA(h, dalloc(&h->d_chunk_state, pop * per));
+         PPI_CUDA(h, dalloc(&h->d_chunk_done, pop));
+         h->chunk_cap = pop * per;
+      }
+   }
    h->geo = g;
    return PPI_OK;
 }
@@ -146,6 +168,8 @@ ppi_status device_status(ppi_gpu* h, int bits) {
       return fail(h, PPI_ERR_DEVICE_STATUS, "a tile copy did not complete (bounded wait expired)");
    if (bits & kStatusBadInstruction)
       return fail(h, PPI_ERR_DEVICE_STATUS, "a kernel met an instruction outside its opcode set");
+   if (bits & kStatusChunkWait)
+      return fail(h, PPI_ERR_DEVICE_STATUS, "a record chunk's predecessor did not finish (bounded wait expired)");
    if (bits & kStatusUnsupportedProgram)
       return fail(h, PPI_ERR_UNSUPPORTED,
                   "a malformed program needs a deeper stack than the generic interpreter's");
@@ -204,19 +228,24 @@ ppi_status enqueue(ppi_gpu* h, const int32_t* d_ph, const float* d_eph, const in
    e.strategy = h->cfg.strategy; e.lanes = h->lanes; e.fitness = d_fit; e.best_key = h->d_key;
    e.stats = h->d_stats; e.best_index = d_best; e.status = h->d_status;
    e.wide_list = h->d_wide;
+   e.chunk_records = g.chunk_records; e.n_chunks = g.n_chunks;
+   e.chunk_state = h->d_chunk_state; e.chunk_done = h->d_chunk_done;
    if (const char* why = best_geometry(h->cfg.best_rule, h->best_group, h->cfg.strategy, n, &e.best))
       return fail(h, PPI_ERR_UNSUPPORTED, why);
+   // work items: programs, or (program, record chunk) pairs
+   const int work = (int)std::min<long long>((long long)n * g.n_chunks, 1LL << 30);
    PPI_CUDA(h, cudaEventRecord(h->ev0, s));
    PPI_CUDA(h, cudaMemsetAsync(h->d_stats, 0, sizeof(DevStats), s));
+   if (g.chunked) PPI_CUDA(h, cudaMemsetAsync(h->d_chunk_done, 0, (size_t)n * sizeof(unsigned), s));
    PPI_CUDA(h, launch_translate(h->cfg.math, t, s));
    h->last_n = n;
    PPI_CUDA(h, cudaEventRecord(h->evm, s));
    e.rows = g.rows; e.wide_pass = 0; e.final_pass = g.wide ? 0 : 1;
-   PPI_CUDA(h, launch_evaluate(h->cfg.math, g.opset, g.main_kernel, e, g.block, std::min(g.grid, n), g.smem, s));
+   PPI_CUDA(h, launch_evaluate(h->cfg.math, g.opset, g.main_kernel, e, g.block, std::min(g.grid, work), g.smem, s));
    h->last_launches = 2;
    if (g.wide) {
       e.rows = g.rows_wide; e.wide_pass = 1; e.final_pass = 1;
-      PPI_CUDA(h, launch_evaluate(h->cfg.math, g.opset, g.wide_kernel, e, g.block, std::min(g.grid_wide, n),
+      PPI_CUDA(h, launch_evaluate(h->cfg.math, g.opset, g.wide_kernel, e, g.block, std::min(g.grid_wide, work),
                                   g.smem_wide, s));
       h->last_launches = 3;
    }
@@ -612,6 +641,15 @@ ppi_status ppi_gpu_last_kernel_ms(ppi_gpu* h, float* ms) {
 }
 
 int32_t ppi_gpu_last_launch_count(const ppi_gpu* h) { return h ? h->last_launches : 0; }
+
+ppi_status ppi_gpu_geometry(const ppi_gpu* h, int32_t* block, int32_t* rows, int32_t* n_chunks) {
+   if (!h) return PPI_ERR_INVALID_ARGUMENT;
+   if (!h->have_data) return PPI_ERR_NOT_READY;
+   if (block) *block = h->geo.block;
+   if (rows) *rows = h->geo.rows;
+   if (n_chunks) *n_chunks = h->geo.n_chunks;
+   return PPI_OK;
+}
 
 int32_t ppi_gpu_lanes(const ppi_gpu* h) { return (h && h->have_data) ? h->lanes : 0; }
 

@@ -32,9 +32,18 @@ enum : int { kOpsetFull = 0, kOpsetArith = 1 };
 // pass, 1 / 2 the wide pass (direct column reads: any tile / whole quads),
 // kMainHi the main pass built for 8 resident CTAs per SM (64 registers); with
 // kOneLane added, the same kernel with the one-lane chain (launches holding a
-// PP population, or PDP over one lane).
+// PP population, or PDP over one lane); with kChunked added, the same kernel
+// walking record chunks in chunk-major order (one PDP population over a
+// dataset larger than L2).
 constexpr int kMainHi = 3;
 constexpr int kOneLane = 4;
+constexpr int kChunked = 8;
+// Kernel families (the template parameter FAMILY of the evaluator kernels).
+enum : int { kFamilyPlain = 0, kFamilyOneLane = 1, kFamilyChunked = 2 };
+// Chunked family: records per work item (tiles of 1024 records) and the
+// smallest dataset (bytes of its columns) it is used for.
+constexpr int kChunkTiles = 64;
+constexpr size_t kChunkMinBytes = (size_t)64 << 20;
 
 // Program kinds written by the translator.  meta.x = kind | rows << 8, where
 // rows is the number of shared-memory rows the program's tile needs; meta.y is
@@ -72,8 +81,11 @@ struct DevStats {
 
 // Status bits reported by the kernels: a program the generic interpreter
 // cannot hold; a tile copy that did not complete within the bounded wait (the
-// CTA stopped); an instruction outside the running kernel's opcode set.
-enum : int { kStatusUnsupportedProgram = 1, kStatusStageTimeout = 2, kStatusBadInstruction = 4 };
+// CTA stopped); an instruction outside the running kernel's opcode set; a
+// record chunk whose predecessor did not finish within the bounded wait (the
+// CTA stopped).
+enum : int { kStatusUnsupportedProgram = 1, kStatusStageTimeout = 2, kStatusBadInstruction = 4,
+             kStatusChunkWait = 8 };
 
 // Accumulator-machine instructions.  Each is a uint2: .x = instruction id
 // below, .y = immediate: float bits of a constant, or a row index.
@@ -414,6 +426,12 @@ struct EvalArgs {
    const int* wide_list;
    int final_pass;             // this pass writes the best index
    BestGeo best;               // best-index rule
+   // chunked family: records per chunk, chunks per program, each program's
+   // lane state between chunks ((R + 1) x block floats) and its finished
+   // chunk count (zeroed before the launch)
+   int chunk_records, n_chunks;
+   float* chunk_state;
+   unsigned* chunk_done;
 };
 
 struct BatchArgs {
@@ -527,14 +545,17 @@ struct Geometry {
    int per_sm[2] = {0, 0};     // resident CTAs per SM of the two passes
    int wide_kernel = 1;        // direct-read kernel of the wide pass: 2 whole quads (PP, PDP), 1 any tile
    int main_kernel = 0;        // kernel of the main pass: 0, or kMainHi when its tile fits more CTAs
-                               //   (both with kOneLane added for one lane)
+                               //   (both with kOneLane added for one lane, kChunked when chunked)
+   bool chunked = false;       // record chunks in chunk-major order (kChunked kernels)
+   int chunk_records = 0, n_chunks = 1;
 };
 // kOpsetArith when every op of the symbol table is in the ARITH set.
 int opset_for(const ppi_symbol_entry* symbols, int n);
 int resolve_lanes(int strategy, int lanes, int nlin, int sm_count);
 // Returns nullptr on success, else why the configuration is unsupported.
+// allow_chunk: the caller can hold the chunked family's lane state.
 const char* plan_geometry(int strategy, int lanes, int math, int opset, int nlin, int ncol,
-                          int code_stride, int n_max, int sm_count, Geometry* g);
+                          int code_stride, int n_max, int sm_count, Geometry* g, bool allow_chunk = false);
 // Largest program row count on a dataset of ncol columns.
 inline int max_program_rows(int ncol) { return kSlots + ncol + 1; }
 

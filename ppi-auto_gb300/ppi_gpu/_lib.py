@@ -315,6 +315,12 @@ class Evaluator:
     def lanes(self):
         return int(self._L.ppi_gpu_lanes(self._h))
 
+    def geometry(self):
+        """(threads per CTA, main-pass tile rows, record chunks per program)."""
+        b, r, c = (np.zeros(1, np.int32) for _ in range(3))
+        self._check(self._L.ppi_gpu_geometry(self._h, _i(b), _i(r), _i(c)))
+        return int(b[0]), int(r[0]), int(c[0])
+
     def last_launch_count(self):
         return int(self._L.ppi_gpu_last_launch_count(self._h))
 
