@@ -21,8 +21,9 @@ A step is one evaluation of every population:
           (ppi_gpu_evaluate_device per population), same timing; the line
           asserts bit-identical fitness and best indices;
   e2e   : the batched evaluator through ppi_batch_evaluate with pinned host
-          buffers: H2D of phenotype/ephemeral/size and D2H of fitness + best
-          indices inside the timed region (host wall clock, synchronous call).
+          buffers: the upload of phenotype/ephemeral/size (each row's used
+          prefix, packed by the library) and D2H of fitness + best indices
+          inside the timed region (host wall clock, synchronous call).
 --workload polynomial: the polynomial-regression configuration (100k records,
 30000 genomes decoded on the GPU into programs <= 128 opcodes), one plain
 evaluation per step.
@@ -133,6 +134,18 @@ def profile_value(name, key):
         if line.startswith(key + ":"):
             return float(line.split(":")[1])
     return None
+
+
+def upload_bytes(sz, max_size):
+    """Bytes the library's host entry points send for these programs from
+    pinned rows (upload.cu): the rows as they are up to 64 MB, else sizes,
+    offsets and each row's used prefix of tokens and ephemerals."""
+    n = len(sz)
+    if n * max_size * 8 <= 64 << 20:
+        return n * max_size * 8 + n * 4
+    tokens = int(np.where((sz >= 1) & (sz <= max_size), sz, 0).astype(np.int64).sum())
+    align8 = lambda x: (x + 7) & ~7
+    return align8(n * 4) + n * 8 + align8(tokens * 4) + tokens * 4
 
 
 def profile_traffic(workload):
@@ -562,7 +575,7 @@ def run_batch(args):
                   "speedup_batched_vs_plain": round(value / plain_v, 3),
                   "equal_fitness": bool(equal)},
         "e2e": {"value": round(e2e, 3), "unit": UNIT,
-                "h2d_bytes_per_step": int(ph.nbytes + eph.nbytes + sz.nbytes),
+                "h2d_bytes_per_step": int(upload_bytes(sz, ph.shape[1])),
                 "d2h_bytes_per_step": int(n * 4 + len(pops) * 4 + 4)},
         "gpu_launches": launches,
         "roofline": {"bound": "fp32_issue", "achieved": round(all_ops / world / (kernel_ms / 1e3) / 1e9, 2),
@@ -722,6 +735,7 @@ def run_polynomial(args):
                            args.math, device=local)
     ev.set_dataset(wl.rows)
     ev.set_grammar(wl.grammar)
+    ev_geo = ev.geometry()
     t0 = time.perf_counter()
     ph, eph, sz = ev.decode(wl.genomes, wl.bits_per_gene, wl.bits_per_constant, wl.lo, wl.hi)
     decode_ms = ev.last_kernel_ms()
@@ -801,6 +815,9 @@ def run_polynomial(args):
     eval_mean = float(np.mean(eval_ms))
     achieved = ops_per_step / (eval_mean / 1e3) / 1e9
     traffic = profile_traffic(wl.name)
+    # bytes a step must move at least: the dataset once, the programs in, the
+    # fitness out
+    algorithmic = int(wl.rows.nbytes + ph.nbytes + eph.nbytes + sz.nbytes + n * 4)
     cpu_v, cpu_n, cpu_cores, cpu_t, cpu_fit = cpu_sample(wl, ph, eph, sz, args.cpu_seconds)
     from oracle import pyoracle
     k64 = min(cpu_n, args.fp64_programs)
@@ -819,7 +836,7 @@ def run_polynomial(args):
                        l2="256 MiB buffer written between steps, outside the timed events",
                        decode_ms=round(decode_ms, 3)),
         "e2e": {"value": round(e2e, 3), "unit": UNIT,
-                "h2d_bytes_per_step": int(ph.nbytes + eph.nbytes + sz.nbytes),
+                "h2d_bytes_per_step": int(upload_bytes(sz, ph.shape[1])),
                 "d2h_bytes_per_step": int(n * 4 + 4)},
         "gpu_launches": launches,
         "roofline": {"bound": "fp32_issue", "achieved": round(achieved, 2),
@@ -829,6 +846,10 @@ def run_polynomial(args):
                      "frac_at_median_clock": round(achieved / (sm_count * 128 * clk["sm_mhz"] / 1e3), 4)
                      if clk.get("sm_mhz") else None,
                      "traffic": traffic,
+                     "traffic_unit": "bytes per step (DRAM read + write, ncu)",
+                     "algorithmic_bytes": algorithmic,
+                     "traffic_over_algorithmic": round(traffic / algorithmic, 2) if traffic else None,
+                     "record_chunks": ev_geo[2],
                      "opmix": opmix_roofline(achieved, [(ph, sz, wl.nlin,
                                                          wl.grammar.symbol_table_arrays())])},
         "cpu_baseline": {"value": round(cpu_v, 4), "unit": UNIT, "cores": cpu_cores,
