@@ -346,9 +346,8 @@ ppi_status ppi_batch_set_shape(ppi_batch* b, int32_t block, int32_t rows);
  * (about 16,000 programs of max_size 128), or a symbol table spanning more
  * than 2^22 values, is rejected with PPI_ERR_UNSUPPORTED and a message on
  * stderr.  The first call on each device looks up the array's device address
- * and caches the launch geometry, so make that first call before any stream
- * capture.  All calls share the array: calls that overlap on the GPU race, so
- * serialise them.  d_status (device memory, may be NULL) receives the
+ * (cudaGetSymbolAddress) and caches the launch geometry.  All calls share the
+ * array: calls that overlap on the GPU race, so serialise them.  d_status (device memory, may be NULL) receives the
  * kernels' status bits once the call's work is done: 0 when every program
  * ran; 1 a malformed program needs a deeper stack than the generic
  * interpreter's (its fitness is FLT_MAX); 2 a tile copy did not complete

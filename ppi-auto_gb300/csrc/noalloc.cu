@@ -16,8 +16,7 @@
 // GPU that loads the library holds it until the process exits.  Host code
 // cannot use the array's name as a device address.  So the first call on each
 // device, with that device current, looks up its address with
-// cudaGetSymbolAddress and keeps it.  That first call per device should
-// therefore happen before any stream capture begins.
+// cudaGetSymbolAddress and keeps it.
 //
 // All calls share the one array, and each call leaves its contents behind.
 // The translator rewrites everything the evaluator reads and resets the
