@@ -82,7 +82,7 @@ struct BatchGeo {
    int rows = 1, grid = 1, per_sm = 1;
    int fit = 1;                        // most rows any tile can have
    size_t smem = 0;
-   int rows_wide = 1, grid_wide = 1;
+   int rows_wide = 1, grid_wide = 1, per_sm_wide = 1;
    size_t smem_wide = 0;
    bool wide = false;
    int wide_kernel = 1;                // 2: every population PP or PDP (whole-quad direct reads)
@@ -181,7 +181,7 @@ void bfree_all(ppi_batch* b) {
 // (the rest, on the kernel with direct column reads): the most rows at its
 // own top occupancy, and at least room for the deepest slot need and the
 // target.
-ppi_status batch_geometry(ppi_batch* b, int P, int rows_req, BatchGeo* g) {
+ppi_status batch_geometry(ppi_batch* b, int P, int rows_req, BatchGeo* g, int rows_wide_req = 0) {
    for (const PopDesc& p : b->host_pops)
       if (p.strategy == PPI_STRATEGY_DP && p.lanes > P * kR)
          return bfail(b, PPI_ERR_UNSUPPORTED, "DP lanes larger than the tile");
@@ -229,7 +229,10 @@ ppi_status batch_geometry(ppi_batch* b, int P, int rows_req, BatchGeo* g) {
       return bfail(b, PPI_ERR_UNSUPPORTED, "evaluator does not fit on an SM");
    int rows = best_rows(0);
    if (rows_req > 0) rows = std::min(rows_req, fit);
-   const int rows2 = std::max(best_rows(wk), std::min(fit, kSlots + 1));
+   // wide pass: rows_wide_req when > 0 (the autotuner's candidates), else the
+   // most rows at its top occupancy and room for the deepest slot need
+   const int rows2 = rows_wide_req > 0 ? std::min(rows_wide_req, fit)
+                                       : std::max(best_rows(wk), std::min(fit, kSlots + 1));
    g->block = P;
    g->fit = fit;
    g->rows = rows;
@@ -241,7 +244,8 @@ ppi_status batch_geometry(ppi_batch* b, int P, int rows_req, BatchGeo* g) {
    g->grid = std::max(1, std::min(b->total, g->per_sm * b->sm_count));
    g->rows_wide = rows2;
    g->smem_wide = smem_for(rows2);
-   g->grid_wide = std::max(1, std::min(b->total, std::max(1, occupancy(wk, rows2)) * b->sm_count));
+   g->per_sm_wide = occupancy(wk, rows2);
+   g->grid_wide = std::max(1, std::min(b->total, std::max(1, g->per_sm_wide) * b->sm_count));
    g->wide = rows < rows_max;
    g->wide_kernel = wk | one;
    return PPI_OK;
@@ -299,10 +303,28 @@ std::vector<int> row_levels(ppi_batch* b, int P) {
    return out;
 }
 
+// Wide-pass row budgets for a shape: the most rows at each of the three best
+// occupancy levels of the wide pass (fewer rows stage fewer columns and read
+// more directly, but let more CTAs run).
+std::vector<int> wide_row_levels(ppi_batch* b, const BatchGeo& base) {
+   std::vector<int> out;
+   int prev_occ = -1;
+   for (int rows = 1; rows <= base.fit + 1 && (int)out.size() < 3; ++rows) {
+      BatchGeo t;
+      const bool ok = rows <= base.fit && batch_geometry(b, base.block, base.rows, &t, rows) == PPI_OK;
+      const int occ = ok ? t.per_sm_wide : 0;
+      if (rows > 1 && occ != prev_occ) out.push_back(rows - 1);
+      if (!ok) break;
+      prev_occ = occ;
+   }
+   return out;
+}
+
 // Time the candidate shapes once on these inputs (twice when a step is
 // short) and keep the fastest: for 128-thread CTAs every occupancy level's
 // most rows, for 64-thread CTAs the level with the same shared memory per
-// warp as the best 128-thread shape.
+// warp as the best 128-thread shape; then, for the shape kept, the wide
+// pass's row budget at each of its best occupancy levels.
 ppi_status autotune(ppi_batch* b, const int32_t* ph, const float* eph, const int32_t* size, float* fit,
                     int32_t* best, cudaStream_t s) {
    auto time_once = [&](const BatchGeo& g, float* ms) -> ppi_status {
@@ -357,6 +379,21 @@ ppi_status autotune(ppi_batch* b, const int32_t* ph, const float* eph, const int
       if ((st = rounds(cand.size() - 1)) != PPI_OK) return st;
       b->tune_ms[0] = best_of.back();
       if (best_of.back() < best_of[pick]) pick = cand.size() - 1;
+   }
+   if (cand[pick].wide) {
+      const size_t from = cand.size();
+      const BatchGeo kept = cand[pick];
+      for (int r2 : wide_row_levels(b, kept)) {
+         BatchGeo g;
+         if (r2 == kept.rows_wide || batch_geometry(b, kept.block, kept.rows, &g, r2) != PPI_OK) continue;
+         cand.push_back(g);
+         best_of.push_back(-1.0f);
+      }
+      if (cand.size() > from) {
+         if ((st = rounds(from)) != PPI_OK) return st;
+         for (size_t c = from; c < cand.size(); ++c)
+            if (best_of[c] < best_of[pick]) pick = c;
+      }
    }
    b->geo = cand[pick];
    b->tuned = true;
