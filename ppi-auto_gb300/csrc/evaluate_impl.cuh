@@ -771,19 +771,32 @@ __global__ void __launch_bounds__(128, min_ctas_per_sm(MATH, HI)) eval_kernel(co
    j.alpha_free = a.best.alpha_free;
    unsigned* queue = a.wide_pass ? &a.stats->wide_queue : &a.stats->queue;
    const int limit = a.wide_pass ? (int)a.stats->wide : a.n;
-   // chunked kernels: work items (program, record chunk) in chunk-major order,
-   // so that the grid walks the dataset together; a chunk waits (bounded) for
-   // its program's previous chunk, which an earlier item holds
+   // chunked kernels: work items (program, record chunk), the programs in
+   // groups and each group's items in chunk-major order, so that the grid
+   // walks the dataset together while the group's lane states stay in L2; a
+   // chunk waits (bounded) for its program's previous chunk, which an earlier
+   // item holds. The main pass walks every program (skipping the wide ones)
+   // in one group: its few programs' states fit, and a group of them would
+   // leave fewer items between a program's chunks than the grid has CTAs.
    constexpr bool chunked = FAMILY == kFamilyChunked;
    const long long items = chunked ? (long long)limit * a.n_chunks : limit;
+   const int group = a.wide_pass ? a.chunk_group : limit;
    __shared__ int s_wait_failed;
    for (;;) {
       if (tid == 0) s_prog = (int)atomicAdd(queue, 1u);
       __syncthreads();
       const int item = s_prog;
       if (item >= items) break;
-      const int c = chunked ? item / limit : 0;
-      const int k = chunked ? item - c * limit : item;
+      int c = 0, k = item;
+      if constexpr (chunked) {
+         const long long span = (long long)group * a.n_chunks;   // items of a full group
+         const int grp = (int)(item / span);
+         const int first = grp * group;
+         const int gn = min(group, limit - first);
+         const int rem = (int)(item - grp * span);
+         c = rem / gn;
+         k = first + rem - c * gn;
+      }
       const int prog = a.wide_pass ? a.wide_list[k] : k;
       j.meta = a.meta[prog];
       const int kind = meta_kind(j.meta);

@@ -228,7 +228,7 @@ ppi_status enqueue(ppi_gpu* h, const int32_t* d_ph, const float* d_eph, const in
    e.strategy = h->cfg.strategy; e.lanes = h->lanes; e.fitness = d_fit; e.best_key = h->d_key;
    e.stats = h->d_stats; e.best_index = d_best; e.status = h->d_status;
    e.wide_list = h->d_wide;
-   e.chunk_records = g.chunk_records; e.n_chunks = g.n_chunks;
+   e.chunk_records = g.chunk_records; e.n_chunks = g.n_chunks; e.chunk_group = g.chunk_group;
    e.chunk_state = h->d_chunk_state; e.chunk_done = h->d_chunk_done;
    if (const char* why = best_geometry(h->cfg.best_rule, h->best_group, h->cfg.strategy, n, &e.best))
       return fail(h, PPI_ERR_UNSUPPORTED, why);

@@ -426,10 +426,11 @@ struct EvalArgs {
    const int* wide_list;
    int final_pass;             // this pass writes the best index
    BestGeo best;               // best-index rule
-   // chunked family: records per chunk, chunks per program, each program's
-   // lane state between chunks ((R + 1) x block floats) and its finished
-   // chunk count (zeroed before the launch)
-   int chunk_records, n_chunks;
+   // chunked family: records per chunk, chunks per program, programs per
+   // group (items walk the groups in turn, chunk-major within a group), each
+   // program's lane state between chunks ((R + 1) x block floats) and its
+   // finished chunk count (zeroed before the launch)
+   int chunk_records, n_chunks, chunk_group;
    float* chunk_state;
    unsigned* chunk_done;
 };
@@ -548,6 +549,7 @@ struct Geometry {
                                //   (both with kOneLane added for one lane, kChunked when chunked)
    bool chunked = false;       // record chunks in chunk-major order (kChunked kernels)
    int chunk_records = 0, n_chunks = 1;
+   int chunk_group = 1;        // programs whose lane state and code stay in L2 together
 };
 // kOpsetArith when every op of the symbol table is in the ARITH set.
 int opset_for(const ppi_symbol_entry* symbols, int n);
