@@ -350,7 +350,8 @@ def run_reference(args):
         return 0
     from ppi_gpu import workloads
     g, pops = workloads.uneven_batch(seed=11, n_pops=args.populations,
-                                     pop_range=(256, args.max_programs))
+                                     pop_range=(256, args.max_programs),
+                                     mixed=getattr(args, "mixed", False))
     sym = g.symbol_table_arrays()
     work = float(sum(int(p["size"].sum()) * p["rows"].shape[0] for p in pops))
     # each step: a bounded sample (a slice of every population's programs,
@@ -548,12 +549,15 @@ def run_batch(args):
     cpu_v, cpu_n, cpu_cores, cpu_t, cpu_fits = batch_cpu_sample(pops, sym, args.cpu_fraction,
                                                                 sm_count=sm_count)
     parity = batch_parity(pops, sym, fit_b, cpu_fits, offs)
-    # issue activity of the evaluator kernels over one step of this same
-    # configuration (launch-list capture), else of the mid-size profile
-    issue = profile_value("launches_uneven-batch", "issue_active_frac")
-    if issue is None:
+    # issue activity and DRAM traffic of the evaluator kernels over one step
+    # of this same configuration (its launch-list capture); the PDP batch
+    # falls back to its mid-size profile for the issue activity
+    mixed = getattr(args, "mixed", False)
+    profile = "uneven-mixed" if mixed else "uneven-batch"
+    issue = profile_value("launches_" + profile, "issue_active_frac")
+    if issue is None and not mixed:
         issue = profile_value("eval_batch_kernel_uneven-batch-mid", "issue_active_frac")
-    traffic = profile_traffic("uneven-batch")
+    traffic = profile_traffic(profile)
     # bytes a step must move at least: every dataset once, the programs in,
     # the fitness and best indices out
     algorithmic = int(sum(p["rows"].nbytes for p in pops) + ph.nbytes + eph.nbytes + sz.nbytes +
@@ -906,7 +910,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--math", default="fast", choices=["fast", "parity", "native"])
     ap.add_argument("--workload", default="uneven",
-                    choices=["uneven", "polynomial", "iris", "stream", "adjoint"])
+                    choices=["uneven", "uneven-mixed", "polynomial", "iris", "stream", "adjoint"])
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--cpu-fraction", type=float, default=0.015,
                     help="uneven batch: share of every population timed on the CPU")
@@ -925,6 +929,7 @@ def main():
         args.records = 4_000_000
     if args.workload == "iris" and args.population == 30_000:
         args.population = 1000
+    args.mixed = args.workload == "uneven-mixed"
     if args.impl == "reference":
         return run_reference(args)
     if args.workload in ("polynomial", "iris", "stream"):

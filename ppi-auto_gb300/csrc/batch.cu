@@ -221,10 +221,10 @@ ppi_status batch_geometry(ppi_batch* b, int P, int rows_req, BatchGeo* g, int ro
       return rows;
    };
    // whole-quad direct reads need every tile to start on a multiple of 4
-   // records: DP tiles advance by lanes * (T / lanes) records
+   // records: DP tiles advance by lanes * dp_tile_groups(lanes, T) records
    int wk = 2;
    for (const PopDesc& p : b->host_pops)
-      if (p.strategy == PPI_STRATEGY_DP && (p.lanes * ((int)T / p.lanes)) % 4 != 0) wk = 1;
+      if (p.strategy == PPI_STRATEGY_DP && (p.lanes * dp_tile_groups(p.lanes, (int)T)) % 4 != 0) wk = 1;
    if (occupancy(0, 1) < 1 || occupancy(wk, 1) < 1)
       return bfail(b, PPI_ERR_UNSUPPORTED, "evaluator does not fit on an SM");
    int rows = best_rows(0);

@@ -247,9 +247,9 @@ const char* plan_geometry(int strategy, int lanes, int math, int opset, int nlin
    // second pass: the rest, with the columns that do not fit read directly
    // (room at least for the deepest slot need and the target)
    // whole-quad direct reads need tiles that start on a multiple of 4
-   // records: PP and PDP tiles (T records) always do, DP tiles (L * (T / L))
-   // when that is a multiple of 4
-   const int tile_step = strategy == PPI_STRATEGY_DP ? L * ((P * R) / L) : P * R;
+   // records: PP and PDP tiles (T records) always do, DP tiles (whole groups
+   // of L records) when dp_tile_groups found a whole-quad count
+   const int tile_step = strategy == PPI_STRATEGY_DP ? L * dp_tile_groups(L, P * R) : P * R;
    const int wk = tile_step % 4 == 0 ? 2 : 1;
    const int rows2 = std::max(best_rows(wk), std::min(fit, kSlots + 1));
    g->lanes = L;

@@ -542,7 +542,7 @@ __device__ float evaluate_program(const Job& j, uint2* s_code, float* s_tile, in
    // reuse the start of the rows region once the last tile is done
    float* s_acc = aligned ? s_tile : s_tile + (size_t)j.rows_cap * T;
    unsigned char* s_done = reinterpret_cast<unsigned char*>(s_acc + L);
-   const int Teff = dp ? L * (T / L) : T;
+   const int Teff = dp ? L * dp_tile_groups(L, T) : T;
    const float fnlin = (float)j.nlin;
    // one lane (PP, or PDP over one lane) in a one-lane kernel: the tile's
    // first non-finite error, found by every thread

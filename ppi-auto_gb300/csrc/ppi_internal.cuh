@@ -26,6 +26,20 @@ constexpr int kGenericStack = 128;
 // Column stride of the device dataset is a multiple of this.
 constexpr int kColumnPad = 1024;
 
+// DP groups (L consecutive records each, reduced by their own tree and then
+// added in record order) per tile of T record slots: the most that fit,
+// rounded down so that the tile is a whole number of 4-record quads, so that
+// every tile starts on a multiple of 4 records (bulk-copy staging and the
+// whole-quad direct reads); the most that fit when no such count does (L
+// above T / 4 and not a multiple of 4). Tiles hold whole groups either way,
+// so the sums do not depend on the count.
+__host__ __device__ inline int dp_tile_groups(int L, int T) {
+   const int fit = T / L;
+   const int step = (L % 4 == 0) ? 1 : ((L % 2 == 0) ? 2 : 4);   // groups per whole-quad tile step
+   const int quads = fit / step * step;
+   return quads > 0 ? quads : fit;
+}
+
 // Opcode sets of the evaluator's bytecode path (evaluate_impl.cuh).
 enum : int { kOpsetFull = 0, kOpsetArith = 1 };
 // Evaluator kernel ids (the `direct` argument of the launchers): 0 the main

@@ -206,14 +206,16 @@ def _sum_of_columns(gen, cols):
 
 
 @pytest.mark.parametrize("strat,lanes", [("PDP", 0), ("PP", 0), ("DP", 64), ("DP", 7), ("DP", 5),
-                                         ("PDP", 100)])
+                                         ("DP", 6), ("DP", 301), ("PDP", 100)])
 def test_wide_dataset_staged_and_direct_columns(gpu_lib, oracle_lib, strat, lanes):
     """A 90-column dataset: programs reading a few columns stage them all in
     the tile; programs reading 12-85 distinct columns stage the most-read
     ones and read the rest directly from global memory (whole 16-byte quads
-    where every tile starts on a multiple of 4 records; DP over 5 lanes steps
-    by 255 records, so its reads take the ragged, scalar path).  Two
-    evaluations in a row must both match the oracle bit for bit."""
+    where every tile starts on a multiple of 4 records: DP tiles hold a
+    whole-quad number of groups, 48 groups of 5 lanes or 42 of 6 in a tile
+    of 256 slots; DP over 301 lanes steps by 301 records, so its reads take
+    the ragged, scalar path).  Two evaluations in a row must both match the
+    oracle bit for bit."""
     d = load_golden("allops")
     rng = np.random.default_rng(77 + lanes)
     rows = _dataset(rng, 3000, 90)
