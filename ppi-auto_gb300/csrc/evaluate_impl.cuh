@@ -66,8 +66,9 @@ struct Direct {
 // staged row has them).  Kernels built with D = 0 run only programs whose
 // columns are all staged, and carry no code for direct reads; D = 2 reads
 // whole 16-byte quads only (tiles that start on a multiple of 4 records: PP,
-// PDP, and DP when lanes * (T / lanes) is one), D = 1 also the ragged ones.  The scalar path's code, unused in PP and
-// PDP, cost the wide pass 7 % (instruction-cache misses) before D = 2.
+// PDP, and DP when dp_tile_groups found a whole-quad group count), D = 1
+// also the ragged ones.  The scalar path's code, unused in PP and PDP, cost
+// the wide pass 7 % (instruction-cache misses) before D = 2.
 template <int D, int R>
 __device__ __forceinline__ void load_operand(uint32_t imm, const float* mine, int T, int P, int tid,
                                              const Direct& g, float (&x)[R]) {
