@@ -588,6 +588,7 @@ struct ProgramUpload {
    void* h_stage = nullptr;   // pinned
    void* d_stage = nullptr;
    size_t cap = 0;
+   cudaEvent_t copied = nullptr;   // after the last copy out of h_stage
 };
 cudaError_t upload_programs(ProgramUpload* u, const int32_t* ph, const float* eph, const int32_t* size,
                             int n, int max_size, int32_t* d_ph, float* d_eph, int32_t* d_size,

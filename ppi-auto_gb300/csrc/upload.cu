@@ -47,6 +47,11 @@ __global__ void expand_programs(const int32_t* __restrict__ sizes, const long lo
 }  // namespace
 
 void free_upload(ProgramUpload* u) {
+   if (u->copied) {   // the last copy out of the pinned area first
+      cudaEventSynchronize(u->copied);
+      cudaEventDestroy(u->copied);
+      u->copied = nullptr;
+   }
    cudaFreeHost(u->h_stage);
    cudaFree(u->d_stage);
    u->h_stage = nullptr;
@@ -83,6 +88,13 @@ cudaError_t upload_programs(ProgramUpload* u, const int32_t* ph, const float* ep
       const int sz = size[i];
       if (sz >= 1 && sz <= max_size) total += sz;
    }
+   // The host rewrites the pinned area below, outside the stream's order: a
+   // copy out of it that an earlier call queued (and whose caller did not
+   // wait, e.g. after a failed launch) must have finished first.
+   if (u->copied) {
+      const cudaError_t e = cudaEventSynchronize(u->copied);
+      if (e != cudaSuccess) return e;
+   }
    const size_t o_off = align8((size_t)n * 4);
    const size_t o_tok = o_off + (size_t)n * 8;
    const size_t o_eph = o_tok + align8((size_t)total * 4);
@@ -98,6 +110,10 @@ cudaError_t upload_programs(ProgramUpload* u, const int32_t* ph, const float* ep
          return e;
       }
       u->cap = cap;
+   }
+   if (!u->copied) {
+      const cudaError_t e = cudaEventCreateWithFlags(&u->copied, cudaEventDisableTiming);
+      if (e != cudaSuccess) return e;
    }
    unsigned char* hs = static_cast<unsigned char*>(u->h_stage);
    std::memcpy(hs, size, (size_t)n * 4);
@@ -128,6 +144,7 @@ cudaError_t upload_programs(ProgramUpload* u, const int32_t* ph, const float* ep
       for (std::thread& th : pool) th.join();
    }
    cudaError_t e = cudaMemcpyAsync(u->d_stage, u->h_stage, bytes, cudaMemcpyHostToDevice, s);
+   if (e == cudaSuccess) e = cudaEventRecord(u->copied, s);
    if (e != cudaSuccess) return e;
    const unsigned char* ds = static_cast<const unsigned char*>(u->d_stage);
    const int block = 256;
