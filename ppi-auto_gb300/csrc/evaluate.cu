@@ -201,8 +201,12 @@ const char* plan_geometry(int strategy, int lanes, int math, int opset, int nlin
    // lane == tile position over a dataset larger than L2: the chunked kernels
    // (every program walks the same records at about the same time, so a
    // record chunk comes from DRAM once and from L2 for the other programs)
+   // (work items are counted in 32 bits: populations whose (program, chunk)
+   // pairs pass 2^30 run unchunked)
+   const long long chunk_recs = (long long)kChunkTiles * P * R;
    const bool chunk = allow_chunk && strategy == PPI_STRATEGY_PDP && aligned_for(P) &&
-                      (size_t)nlin * ncol * 4 >= kChunkMinBytes;
+                      (size_t)nlin * ncol * 4 >= kChunkMinBytes &&
+                      (long long)n_max * ((nlin + chunk_recs - 1) / chunk_recs) < (1LL << 30);
    const int one = strategy != PPI_STRATEGY_DP && L == 1 ? kOneLane : (chunk ? kChunked : 0);
    auto occupancy = [&](int direct, int rows) {
       int per_sm = 0;
