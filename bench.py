@@ -849,6 +849,7 @@ def run_polynomial(args):
                      "kernel": "eval_kernel", "kernel_ms": round(eval_mean, 4),
                      "frac_at_median_clock": round(achieved / (sm_count * 128 * clk["sm_mhz"] / 1e3), 4)
                      if clk.get("sm_mhz") else None,
+                     "issue_active_frac": profile_value("launches_" + wl.name, "issue_active_frac"),
                      "traffic": traffic,
                      "traffic_unit": "bytes per step (DRAM read + write, ncu)",
                      "algorithmic_bytes": algorithmic,
