@@ -789,15 +789,7 @@ __global__ void __launch_bounds__(128, min_ctas_per_sm(MATH, HI)) eval_kernel(co
       const int item = s_prog;
       if (item >= items) break;
       int c = 0, k = item;
-      if constexpr (chunked) {
-         const long long span = (long long)group * a.n_chunks;   // items of a full group
-         const int grp = (int)(item / span);
-         const int first = grp * group;
-         const int gn = min(group, limit - first);
-         const int rem = (int)(item - grp * span);
-         c = rem / gn;
-         k = first + rem - c * gn;
-      }
+      if constexpr (chunked) chunk_item(item, limit, group, a.n_chunks, &c, &k);
       const int prog = a.wide_pass ? a.wide_list[k] : k;
       j.meta = a.meta[prog];
       const int kind = meta_kind(j.meta);

@@ -26,6 +26,22 @@ constexpr int kGenericStack = 128;
 // Column stride of the device dataset is a multiple of this.
 constexpr int kColumnPad = 1024;
 
+// Work item of the chunked kernels -> (record chunk c, program k): the
+// programs in groups of `group`, each group's items chunk-major (the last
+// group may be smaller). Every (c, k) with c < n_chunks, k < limit is one
+// item of [0, limit * n_chunks), and (c - 1, k) always has a smaller index,
+// so a chunk's wait is on an item an earlier CTA took from the queue.
+__host__ __device__ inline void chunk_item(long long item, int limit, int group, int n_chunks,
+                                           int* c, int* k) {
+   const long long span = (long long)group * n_chunks;   // items of a full group
+   const int grp = (int)(item / span);
+   const int first = grp * group;
+   const int gn = limit - first < group ? limit - first : group;
+   const int rem = (int)(item - grp * span);
+   *c = rem / gn;
+   *k = first + rem - *c * gn;
+}
+
 // DP groups (L consecutive records each, reduced by their own tree and then
 // added in record order) per tile of T record slots: the most that fit,
 // rounded down so that the tile is a whole number of 4-record quads, so that
