@@ -200,9 +200,9 @@ const char* plan_geometry(int strategy, int lanes, int math, int opset, int nlin
    // one lane (PP, or PDP over one lane): the kernels with the one-lane chain;
    // lane == tile position over a dataset larger than L2: the chunked kernels
    // (every program walks the same records at about the same time, so a
-   // record chunk comes from DRAM once and from L2 for the other programs)
-   // (work items are counted in 32 bits: populations whose (program, chunk)
-   // pairs pass 2^30 run unchunked)
+   // record chunk comes from DRAM once and from L2 for the other programs),
+   // when the population's (program, chunk) pairs fit the kernels' 32-bit
+   // work counter (2^30 of them)
    const long long chunk_recs = (long long)kChunkTiles * P * R;
    const bool chunk = allow_chunk && strategy == PPI_STRATEGY_PDP && aligned_for(P) &&
                       (size_t)nlin * ncol * 4 >= kChunkMinBytes &&
