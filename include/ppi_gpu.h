@@ -185,7 +185,11 @@ ppi_status ppi_gpu_evaluate(ppi_gpu* h, const int32_t* phenotype, const float* e
 
 /* The same call split in two: launch copies the inputs and starts the kernels;
  * wait blocks until they finish and fills fitness / best_index (the pointers
- * given to launch must stay valid until wait returns). */
+ * given to launch must stay valid until wait returns).  Programs in pageable
+ * memory (PPI's own arrays) are packed on the host before launch returns and
+ * may be changed at once; programs in pinned memory of at most 64 MB of rows
+ * are read by the asynchronous copy itself and must stay unchanged until wait
+ * returns. */
 ppi_status ppi_gpu_evaluate_launch(ppi_gpu* h, const int32_t* phenotype, const float* ephemeral,
                                    const int32_t* size, int32_t n, float alpha, float* fitness,
                                    int32_t* best_index);
