@@ -26,6 +26,8 @@
 //     the wide pass the few that need more rows.
 #pragma once
 
+#include <atomic>
+
 #include "ppi_internal.cuh"
 
 namespace ppi {
@@ -996,18 +998,24 @@ struct Launch {
    static PredictFn predict_fn(int opset) {
       return opset ? predict_kernel<MATH, kR, kOpsetArith> : predict_kernel<MATH, kR, kOpsetFull>;
    }
-   // Allow up to 200 KB of dynamic shared memory, once per kernel.
+   // Allow up to 200 KB of dynamic shared memory, once per kernel and device
+   // (a function's attributes belong to each device's context; devices past
+   // the first 64 set them on every call).
    static cudaError_t configure(int opset) {
-      static bool done[2] = {false, false};
-      if (done[opset]) return cudaSuccess;
+      static std::atomic<unsigned long long> done[2];
+      int dev = 0;
+      cudaError_t e = cudaGetDevice(&dev);
+      if (e != cudaSuccess) return e;
+      const unsigned long long bit = dev >= 0 && dev < 64 ? 1ull << dev : 0ull;
+      if (bit & done[opset].load(std::memory_order_acquire)) return cudaSuccess;
       const int attr = cudaFuncAttributeMaxDynamicSharedMemorySize, bytes = 200 * 1024;
       for (int direct = 0; direct <= kMainHi; ++direct) {
-         cudaError_t e = cudaFuncSetAttribute(eval_fn(opset, direct), (cudaFuncAttribute)attr, bytes);
+         e = cudaFuncSetAttribute(eval_fn(opset, direct), (cudaFuncAttribute)attr, bytes);
          if (e == cudaSuccess) e = cudaFuncSetAttribute(batch_fn(opset, direct), (cudaFuncAttribute)attr, bytes);
          if (e != cudaSuccess) return e;
       }
-      cudaError_t e = cudaFuncSetAttribute(predict_fn(opset), (cudaFuncAttribute)attr, bytes);
-      if (e == cudaSuccess) done[opset] = true;
+      e = cudaFuncSetAttribute(predict_fn(opset), (cudaFuncAttribute)attr, bytes);
+      if (e == cudaSuccess) done[opset].fetch_or(bit, std::memory_order_release);
       return e;
    }
    static cudaError_t evaluate(int opset, int direct, const EvalArgs& a, int block, int grid, size_t smem,
