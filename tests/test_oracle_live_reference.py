@@ -7,10 +7,17 @@ over any lane count, and its GPU tests compare with the oracle there.
 Here the oracle meets the reference's accelerator.cl (compiled as C++ by
 oracle/build_ref.py) on the fixtures' programs and datasets at those lane
 counts: fitness bit for bit, and the index best_individual + PickNBest
-return (work-groups of 16 programs)."""
+return (work-groups of 16 programs).
+
+The fixtures also hold 96 decoded programs each; random programs from the
+tests' generator (every opcode of the grammar, nesting up to 60 operators,
+within max_size) add the reference's sequential interpreter (fitness, best
+index, predictions) and its OpenCL kernels at the fixtures' own lane
+counts."""
+import numpy as np
 import pytest
 
-from helpers import assert_bitexact, expected_best, load_golden, oracle_for
+from helpers import ProgramGen, assert_bitexact, expected_best, load_golden, oracle_for
 
 DP_LANES = [1, 3, 6, 7, 33, 101]   # 101: one group fills a 256-slot tile, raggedly
 PDP_LANES = [3, 100]
@@ -46,3 +53,39 @@ def test_oracle_equals_reference_kernels(oracle_lib, name):
         assert_bitexact(got, want, "%s %s %d" % (name, strategy, lanes))
         assert expected_best(oracle_lib, o, ph, ep, sz, strategy, lanes, alpha, group=16) == want_best, \
             "%s %s %d best index" % (name, strategy, lanes)
+
+
+def _random_programs(d, n, seed):
+    rng = np.random.default_rng(seed)
+    gen = ProgramGen(d, rng, d["rows"].shape[1])
+    progs = []
+    while len(progs) < n:
+        p = gen.random(int(rng.integers(0, 60)))
+        if len(p) <= d["max_size"]:   # whole programs: the reference reads no missing operand
+            progs.append(p)
+    return ProgramGen.rows(progs, d["max_size"])
+
+
+@pytest.mark.parametrize("name", ["allops", "allops_prot", "allops_sqmax", "cfg5", "random"])
+def test_oracle_equals_reference_on_random_programs(oracle_lib, name):
+    from oracle import pyoracle
+    d = load_golden(name)
+    ref = _ref(name)
+    ph, ep, sz = _random_programs(d, 300, 2026)
+    alpha = float(d["alpha"])
+    # the sequential interpreter (double libm): the oracle's default arithmetic
+    want, want_best = ref.seq_evaluate(d["rows"], ph, ep, sz, alpha=alpha)
+    o = oracle_for(pyoracle, d)
+    got = o.evaluate(ph, ep, sz, "PP", 1, alpha)
+    assert_bitexact(got, want, "%s sequential" % name)
+    assert oracle_lib.best_index(got) == want_best
+    for i in range(0, len(sz), 50):
+        p_, _ = ref.seq_evaluate(d["rows"], ph[i:i + 1], ep[i:i + 1], sz[i:i + 1], prediction=True)
+        assert_bitexact(o.predict(ph[i], ep[i], sz[i]), p_, "%s prediction %d" % (name, i))
+    # the OpenCL kernels (float math functions) at the fixtures' lane counts
+    of = oracle_for(pyoracle, d, float_math=True)
+    for strategy, lanes in [("PP", 16), ("PDP", 7), ("DP", 5)]:
+        want, want_best = ref.cl_evaluate(strategy, d["rows"], ph, ep, sz, lanes, 16, alpha=alpha)
+        assert_bitexact(of.evaluate(ph, ep, sz, strategy, lanes, alpha), want,
+                        "%s %s %d" % (name, strategy, lanes))
+        assert expected_best(oracle_lib, of, ph, ep, sz, strategy, lanes, alpha, group=16) == want_best
