@@ -13,11 +13,12 @@ The fixtures also hold 96 decoded programs each; random programs from the
 tests' generator (every opcode of the grammar, nesting up to 60 operators,
 within max_size) add the reference's sequential interpreter (fitness, best
 index, predictions) and its OpenCL kernels at the fixtures' own lane
-counts."""
+counts.  And genome decode on fresh random genomes of several lengths,
+bits per gene and constant ranges."""
 import numpy as np
 import pytest
 
-from helpers import ProgramGen, assert_bitexact, expected_best, load_golden, oracle_for
+from helpers import ProgramGen, Tables, assert_bitexact, expected_best, load_golden, oracle_for
 
 DP_LANES = [1, 3, 6, 7, 33, 101]   # 101: one group fills a 256-slot tile, raggedly
 PDP_LANES = [3, 100]
@@ -89,3 +90,24 @@ def test_oracle_equals_reference_on_random_programs(oracle_lib, name):
         assert_bitexact(of.evaluate(ph, ep, sz, strategy, lanes, alpha), want,
                         "%s %s %d" % (name, strategy, lanes))
         assert expected_best(oracle_lib, of, ph, ep, sz, strategy, lanes, alpha, group=16) == want_best
+
+
+@pytest.mark.parametrize("name", ["allops", "cfg2", "cfg5", "iris", "random"])
+def test_oracle_decode_equals_reference_on_random_genomes(oracle_lib, name):
+    d = load_golden(name)
+    ref = _ref(name)
+    rng = np.random.default_rng(77)
+    ms = d["max_size"]
+    for nb, bg, bc, lo, hi in [(400, d["bg"], 8, -1.0, 1.0), (2000, d["bg"], 16, -10.0, 10.0),
+                               (6000, d["bg"], 24, -1e3, 5.0)]:
+        genomes = rng.integers(0, 2, (200, nb), dtype=np.uint8)
+        rph, rep, rsz, _ = ref.decode(genomes, bg, bc, lo, hi, ms)
+        ph, ep, sz = oracle_lib.decode(Tables(d), genomes, bg, bc, lo, hi, ms)
+        want = rsz.copy()
+        want[want > ms] = 0   # the reference wrote past max_size: invalid here
+        np.testing.assert_array_equal(sz, want)
+        assert (sz > 0).sum() >= 50, "most genomes should decode to programs"
+        for i in np.nonzero(sz > 0)[0]:
+            np.testing.assert_array_equal(ph[i, :sz[i]], rph[i, :sz[i]])
+            c = (ph[i, :sz[i]] == d["t_const"]) | (ph[i, :sz[i]] == d["t_attribute"])
+            assert_bitexact(ep[i, :sz[i]][c], rep[i, :sz[i]][c], "%s genome %d" % (name, i))
