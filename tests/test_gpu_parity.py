@@ -99,6 +99,28 @@ def test_device_decode_equals_reference(gpu_lib, name):
         assert_bitexact(ep[i, :n][c], d["ephemeral"][i, :n][c], "ephemeral %d" % i)
 
 
+@pytest.mark.parametrize("name", ["allops", "cfg2", "cfg5", "iris", "random"])
+def test_device_decode_equals_oracle_on_random_genomes(gpu_lib, oracle_lib, name):
+    """Fresh random genomes (several lengths, constant widths and ranges):
+    the device decode against the oracle's, itself pinned to the reference's
+    decode on such genomes."""
+    d = load_golden(name)
+    ev = make_evaluator(d, "PDP", 0, "parity", population=200)
+    ev.set_grammar(Tables(d))
+    rng = np.random.default_rng(78)
+    for nb, bc, lo, hi in [(400, 8, -1.0, 1.0), (2000, 16, -10.0, 10.0), (6000, 24, -1e3, 5.0)]:
+        genomes = rng.integers(0, 2, (200, nb), dtype=np.uint8)
+        ph, ep, sz = ev.decode(genomes, d["bg"], bc, lo, hi)
+        oph, oep, osz = oracle_lib.decode(Tables(d), genomes, d["bg"], bc, lo, hi, d["max_size"])
+        np.testing.assert_array_equal(sz, osz)
+        assert (sz > 0).sum() >= 20
+        for i in np.nonzero(sz > 0)[0]:
+            n = sz[i]
+            np.testing.assert_array_equal(ph[i, :n], oph[i, :n])
+            c = (ph[i, :n] == d["t_const"]) | (ph[i, :n] == d["t_attribute"])
+            assert_bitexact(ep[i, :n][c], oep[i, :n][c], "%s genome %d" % (name, i))
+
+
 @pytest.mark.parametrize("name", ["cfg2", "cfg5", "iris"])
 def test_decode_evaluate_matches_separate_calls(gpu_lib, name):
     d = load_golden(name)
