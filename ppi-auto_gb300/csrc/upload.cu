@@ -4,7 +4,7 @@
 // (phenotype) and ephemerals (ppi.cc, acc_interpret's arguments), of which a
 // program uses its first size[i]: on the uneven batch 16 % of the 737 MB.
 // Copying the rows as they are moves the padding too, and from PPI's own
-// (pageable) arrays the driver stages every byte through a bounce buffer.
+// (pageable) arrays the CUDA driver stages every byte through a bounce buffer.
 // Here the used prefixes are packed on the host into a pinned staging area
 // (threads over programs for large populations), copied in one transfer,
 // and scattered back into the device rows by a small kernel; the translator
