@@ -277,10 +277,11 @@ int32_t ppi_gpu_kernel_arch(void);
 ppi_status ppi_gpu_constant_gradient(ppi_gpu* h, const int32_t* phenotype, const float* ephemeral,
                                      const int32_t* size, int32_t n, float* gradient);
 
-/* ---- batches: many populations in one launch ------------------------------
+/* ---- batches: many populations in one step ---------------------------------
  * No single reference function: this evaluates what several acc_interpret
  * calls would (one per population, e.g. one per island or per independent
- * run) in one persistent launch.  Each population keeps its own dataset,
+ * run) in one step: a main and a wide pass, each one persistent launch over
+ * all populations' programs.  Each population keeps its own dataset,
  * strategy, lanes, error function, REDUCEMAX and PROTECTED settings, and its
  * fitness values are bit-identical to ppi_gpu_evaluate on that population
  * alone. */

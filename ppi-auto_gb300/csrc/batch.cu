@@ -1,4 +1,4 @@
-// batch.cu -- many populations evaluated by one persistent launch.
+// batch.cu -- many populations evaluated together, one persistent launch per pass.
 //
 // A GE run with several islands, or several independent runs, has
 // populations of very different sizes, program lengths and datasets.  One
@@ -6,7 +6,7 @@
 // ones and pays a tail on every launch.  Here all programs of all populations
 // form one work queue, ordered by cost (size x records, largest first, via
 // 64 power-of-two buckets counted by the translator), and one persistent grid
-// drains it.  Each population keeps its own strategy, lane count, error
+// per pass drains it.  Each population keeps its own strategy, lane count, error
 // function and accumulation order, so every fitness is bit-identical to the
 // plain evaluation of that population.
 //

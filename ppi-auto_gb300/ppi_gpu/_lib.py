@@ -326,7 +326,7 @@ class Evaluator:
 
 
 class BatchEvaluator:
-    """Many populations in one launch (ppi_batch_* of the C ABI).
+    """Many populations in one batched step (ppi_batch_* of the C ABI).
 
     pops: list of dicts with keys rows, n and optionally strategy, lanes,
     error_fn, cost, reduce_max, protected.  Programs, fitness: all
