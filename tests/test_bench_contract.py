@@ -1,6 +1,6 @@
 """bench.py's reference arm (CPU only): the JSON line it prints for a
-single-population workload, and the `unavailable` line for the workload the
-reference has no counterpart of."""
+single-population workload and for the mixed-settings batch, and the
+`unavailable` line for the workload the reference has no counterpart of."""
 import json
 import os
 import subprocess
@@ -32,3 +32,13 @@ def test_reference_arm_line_iris():
 def test_reference_arm_adjoint_is_unavailable():
     d = _run("--workload", "adjoint", "--steps", "1", "--warmup", "0")
     assert d["impl"] == "reference" and "unavailable" in d
+
+
+def test_reference_arm_mixed_batch_names_its_workload():
+    """The mixed-settings batch (strategy, error function and reduction drawn
+    per population) on the CPU: the same populations as the GPU arm's
+    `uneven-mixed` workload, named so."""
+    d = _run("--workload", "uneven-mixed", "--steps", "1", "--warmup", "0", "--cpu-fraction", "0.001")
+    assert d["impl"] == "reference" and d["value"] > 0
+    assert d["config"]["workload"].endswith("-mixed")
+    assert d["cpu_baseline"]["kind"] == "port"
